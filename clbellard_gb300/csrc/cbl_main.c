@@ -1,0 +1,160 @@
+/*
+ * cbl_main.c - command-line driver over libclbellard.so, taking the roles of
+ * CLBellard.exe (normal mode and work mode, Bellard_192.hsp) and
+ * workmodeSum0_6.exe (workmodeSum0_6.hsp) without the GUI.
+ *
+ *   cbl normal <digits> [precision 0|1|2] [device]
+ *   cbl work   <worklist.txt> [workdir] [device]
+ *   cbl sum    [workdir]
+ *   cbl hexpos <p> [device]            any hex position p >= 3
+ */
+#include <ctype.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "clbellard.h"
+
+static const uint64_t kBatchSize = 137438953472ull; /* 2^37, Bellard_192.hsp:19 */
+
+static int64_t now_ms(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (int64_t)ts.tv_sec * 1000 + ts.tv_nsec / 1000000;
+}
+
+static int fail(int rc, const char *what)
+{
+    fprintf(stderr, "%s: %s (%d)\n", what, cbl_strerror(rc), rc);
+    return 1;
+}
+
+/* "digits=..." with ',', ' ', '-' removed (Bellard_192.hsp:179-182, 444-447). */
+static uint64_t parse_digits(const char *s)
+{
+    uint64_t v = 0;
+    int any = 0;
+    for (; *s; ++s) {
+        if (isdigit((unsigned char)*s)) {
+            if (v > 99999999999999999ull) return 999999999999999999ull + 1; /* clamp above the limit */
+            v = v * 10 + (uint64_t)(*s - '0');
+            any = 1;
+        }
+    }
+    return any ? v : 0;
+}
+
+static int cmd_normal(int argc, char **argv)
+{
+    if (argc < 3) return fprintf(stderr, "usage: cbl normal <digits> [precision] [device]\n"), 2;
+    uint64_t needD = parse_digits(argv[2]), d, adj;
+    int precision = argc > 3 ? atoi(argv[3]) : 1, device = argc > 4 ? atoi(argv[4]) : 0;
+    int rc = cbl_pos_to_d(needD, &d, &adj);
+    if (rc) return fail(rc, "invalid digits");
+    cbl_ctx *c;
+    if ((rc = cbl_create(device, precision, &c))) return fail(rc, "cbl_create");
+    char name[256], hex[49];
+    cbl_device_name(c, name, sizeof name);
+    printf("%s\ndigits=%llu\nloopnum=%llu\n", name, (unsigned long long)adj, (unsigned long long)d);
+    const int64_t t0 = now_ms();
+    rc = cbl_compute(c, needD, hex);
+    const int64_t t1 = now_ms();
+    if (rc) return cbl_destroy(c), fail(rc, "cbl_compute");
+    printf("All calc time %lldms\nPI value output -> \n%s\n", (long long)(t1 - t0), hex);
+    cbl_destroy(c);
+    return 0;
+}
+
+static int cmd_work(int argc, char **argv)
+{
+    if (argc < 3) return fprintf(stderr, "usage: cbl work <worklist> [workdir] [device]\n"), 2;
+    const char *workdir = argc > 3 ? argv[3] : "work";
+    int device = argc > 4 ? atoi(argv[4]) : 0;
+    FILE *f = fopen(argv[2], "rb");
+    if (!f) return fail(CBL_E_IO, argv[2]);
+    char line[512];
+    uint64_t needD = 0;
+    int precision = -1, ln = 0, rc;
+    cbl_ctx *c = NULL;
+    char name[256] = "";
+    while (fgets(line, sizeof line, f)) {
+        if (ln == 0) {
+            needD = parse_digits(line); /* Bellard_192.hsp:178-182 */
+        } else if (ln == 1) {
+            const char *p = strchr(line, '='); /* first character after "precision=" (:184-189) */
+            p = p ? p + 1 : line;
+            while (*p == ' ') ++p;
+            precision = (*p >= '0' && *p <= '2') ? *p - '0' : -1;
+            if (needD < 5 || needD > 999999999999999999ull || precision < 0) {
+                fclose(f);
+                return fail(CBL_E_FORMAT, "worklist header"); /* Bellard_192.hsp:222-226 */
+            }
+            if ((rc = cbl_create(device, precision, &c))) {
+                fclose(f);
+                return fail(rc, "cbl_create");
+            }
+            cbl_device_name(c, name, sizeof name);
+        } else {
+            /* "s_b" (Bellard_192.hsp:238-244) */
+            if (!isdigit((unsigned char)line[0]) || line[1] != '_') { ++ln; continue; }
+            int s = line[0] - '0';
+            uint64_t b = strtoull(line + 2, NULL, 10);
+            char hex[49];
+            if (cbl_job_read(workdir, s, b, hex) == CBL_OK) { ++ln; continue; } /* done before (:307-308) */
+            const int64_t t0 = now_ms();
+            rc = cbl_run_job(c, needD, s, b, kBatchSize, hex);
+            const int64_t ms = now_ms() - t0;
+            if (rc == CBL_SKIPPED) { ++ln; continue; }
+            if (rc) { fclose(f); cbl_destroy(c); return fail(rc, "cbl_run_job"); }
+            rc = cbl_job_write(workdir, s, b, hex, device, name, ms);
+            if (rc) { fclose(f); cbl_destroy(c); return fail(rc, "cbl_job_write"); }
+            printf("%d_%llu : time=%lldms\n%s\n", s, (unsigned long long)b, (long long)ms, hex);
+        }
+        ++ln;
+    }
+    fclose(f);
+    if (c) cbl_destroy(c);
+    printf("end\n");
+    return 0;
+}
+
+static int cmd_sum(int argc, char **argv)
+{
+    const char *workdir = argc > 2 ? argv[2] : "work";
+    char out[49];
+    int counts[7];
+    int rc = cbl_workdir_sum(workdir, out, counts);
+    if (rc) return fail(rc, "workmode sum");
+    printf("file num\n");
+    for (int s = 0; s < 7; ++s) printf("%d:%d\n", s, counts[s]);
+    printf("\n%s\n", out);
+    return 0;
+}
+
+static int cmd_hexpos(int argc, char **argv)
+{
+    if (argc < 3) return fprintf(stderr, "usage: cbl hexpos <p> [device]\n"), 2;
+    uint64_t p = strtoull(argv[2], NULL, 10);
+    cbl_ctx *c;
+    int rc = cbl_create(argc > 3 ? atoi(argv[3]) : 0, 1, &c);
+    if (rc) return fail(rc, "cbl_create");
+    char hex[49];
+    rc = cbl_compute_hexpos(c, p, hex);
+    cbl_destroy(c);
+    if (rc) return fail(rc, "cbl_compute_hexpos");
+    printf("%s\n", hex);
+    return 0;
+}
+
+int main(int argc, char **argv)
+{
+    if (argc >= 2 && !strcmp(argv[1], "normal")) return cmd_normal(argc, argv);
+    if (argc >= 2 && !strcmp(argv[1], "work")) return cmd_work(argc, argv);
+    if (argc >= 2 && !strcmp(argv[1], "sum")) return cmd_sum(argc, argv);
+    if (argc >= 2 && !strcmp(argv[1], "hexpos")) return cmd_hexpos(argc, argv);
+    fprintf(stderr, "usage: cbl normal|work|sum|hexpos ...\n");
+    return 2;
+}

@@ -1,0 +1,46 @@
+"""Position 1e10 (the benchmark workload) and 1e11 on the GPU against the
+exact oracle fixtures and published digits; overlap at 1e10."""
+import os
+
+import pytest
+
+from conftest import GOLDEN, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def agree(a, b):
+    from oracle.oracle import agreeing_hex_digits
+    return agreeing_hex_digits(a, b)
+
+
+def test_1e10(ctx192):
+    pub = load_golden("published_digits.json")["digits"]
+    h = ctx192.compute(10 ** 10)
+    assert h.startswith(pub["10000000000"])
+    path = os.path.join(GOLDEN, "oracle_big.json")
+    if os.path.exists(path):
+        big = load_golden("oracle_big.json")
+        if "10000000000" in big:
+            assert h == big["10000000000"]["hex192"]           # bit-exact 192-bit definition
+            assert agree(h, big["10000000000"]["hex256"]) >= 30
+
+
+def test_1e10_overlap(ctx192):
+    a = ctx192.compute_hexpos(10 ** 10)
+    b = ctx192.compute_hexpos(10 ** 10 - 8)
+    assert agree(a, b[8:]) >= 24
+
+
+def test_1e9(ctx192):
+    pub = load_golden("published_digits.json")["digits"]
+    h = ctx192.compute(10 ** 9)
+    assert h.startswith(pub["1000000000"])
+    s = load_golden("survey_probe.json")
+    assert agree(h, s["exact256"]["1000000000"]) >= 33
+
+
+def test_1e11(ctx192):
+    pub = load_golden("published_digits.json")["digits"]
+    h = ctx192.compute(10 ** 11)
+    assert h.startswith(pub["100000000000"])

@@ -1,0 +1,57 @@
+"""Per-term parity of the CUDA term kernels with the oracle: every signed
+192-bit term bit-exact, over both residue widths, their boundary, the tail,
+and seeded samples of the benchmark positions."""
+import random
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+W1_MAX = 1 << 28
+
+
+def check_terms(ctx, oracle, d, f, ks):
+    got = ctx.terms(d, f, ks)
+    for k, g in zip(ks, got):
+        assert g == oracle.term(d, f, k, 3), (d, f, k)
+
+
+@pytest.mark.parametrize("f", range(7))
+def test_terms_small_positions(ctx192, oracle, f):
+    for d in (1, 3, 5, 99, 399999):
+        ks = sorted(set([0, 1, 2, d - 1] + list(range(d, d + 30)) + [random.Random(d).randrange(d) for _ in range(50)]))
+        check_terms(ctx192, oracle, d, f, [k for k in ks if k >= 0])
+
+
+@pytest.mark.parametrize("f", range(7))
+def test_terms_width_boundary(ctx192, oracle, f):
+    """k around the first modulus >= 2^28 (width 1 -> width 2)."""
+    den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
+    kw = (W1_MAX - den1 + den0 - 1) // den0
+    d = 3999999999
+    ks = list(range(kw - 40, kw + 40))
+    check_terms(ctx192, oracle, d, f, ks)
+
+
+def test_terms_sampled_1e8(ctx192, oracle):
+    """1e5 seeded n at position 1e8 (all moduli < 2^32), all 7 series."""
+    rng = random.Random(0x5EED)
+    d = 39999999
+    for f in range(7):
+        ks = [rng.randrange(0, d + 20) for _ in range(100000 // 7)]
+        check_terms(ctx192, oracle, d, f, ks)
+
+
+@pytest.mark.parametrize("d", [3999999999, 39999999999, 399999999999])
+def test_terms_sampled_large(ctx192, oracle, d):
+    """Positions 1e10 .. 1e12: moduli up to ~2^42, exponents up to ~2^42."""
+    rng = random.Random(d)
+    for f in range(7):
+        ks = [rng.randrange(0, d) for _ in range(3000)] + [d - 1, d - 2, d, d + 19]
+        check_terms(ctx192, oracle, d, f, ks)
+
+
+def test_terms_reject_modulus_range(ctx192, cbl):
+    with pytest.raises(cbl.CblError) as e:
+        ctx192.terms(1 << 60, 0, [1 << 49])
+    assert e.value.code == -6

@@ -1,0 +1,120 @@
+"""Work-mode host logic on the CPU: worklist format, job files, the
+workmodeSum merge, and sharding jobs over 2 gloo ranks. Job partials come from
+the oracle here (the CPU stands in for the GPUs only in this test)."""
+import os
+
+import pytest
+
+from conftest import load_golden
+
+
+def oracle_job(oracle, batchsize):
+    """The reference's job partial (numer-weighted, 192-bit) from the oracle."""
+    def fn(needD, s, b, bs):
+        d, _ = oracle.pos_to_d(needD)
+        k0, k1 = b * bs, (b + 1) * bs
+        if k0 > d:
+            return None
+        kend = min(k1, d)
+        v = oracle.sum_range(d, s, k0, kend, 3) if k0 < kend else 0
+        if max(k0, kend) == d:                        # tail when the range reaches d
+            v += oracle.sum_range(d, s, d, d + 20, 3)
+        v = (v << oracle.NUMER_LOG2[s]) % (1 << 192)
+        return "%048x" % v
+    return fn
+
+
+def test_parse_sample_worklist():
+    from clbellard_gb300 import workmode as W
+    # the reference's work/worklist_sample.txt layout
+    text = "digits=200000000\r\nprecision=1 (0=106bit , 1=192bit)\r\n0_0\r\n1_0\r\n2_0\r\n3_0\r\n4_0\r\n5_0\r\n6_0"
+    wl = W.parse_worklist(text)
+    assert wl.digits == 200000000 and wl.precision == 1
+    assert wl.jobs == [(s, 0) for s in range(7)]
+    assert W.parse_worklist(W.format_worklist(wl)).jobs == wl.jobs
+    with pytest.raises(ValueError):
+        W.parse_worklist("digits=3\nprecision=1\n")
+    with pytest.raises(ValueError):
+        W.parse_worklist("digits=1000\nprecision=x\n")
+
+
+def test_job_files_roundtrip(tmp_path, cbl):
+    from clbellard_gb300 import workmode as W
+    h = "0123456789abcdef" * 3
+    W.write_job(str(tmp_path), 3, 17, h, 0, "NVIDIA GB300", 1234)
+    raw = open(os.path.join(tmp_path, "3", "3_17.txt"), "rb").read()
+    assert raw == (h + "\r\n0\tNVIDIA GB300\r\n1234ms").encode()
+    assert W.read_job(str(tmp_path), 3, 17) == h
+    assert W.read_job(str(tmp_path), 3, 18) is None
+
+
+def test_workdir_sum_equals_normal_mode(tmp_path, cbl, oracle):
+    """Jobs with a small batch size, merged as workmodeSum does, give the
+    normal-mode result bit for bit."""
+    from clbellard_gb300 import workmode as W
+    needD = 100000
+    d, _ = oracle.pos_to_d(needD)
+    bs = 7919
+    jobs = W.all_jobs(d, bs)
+    n = W.run_jobs(jobs, needD, str(tmp_path), oracle_job(oracle, bs), batchsize=bs)
+    assert n == len(jobs)
+    # a second pass finds every file and runs nothing (Bellard_192.hsp:307-308)
+    assert W.run_jobs(jobs, needD, str(tmp_path), oracle_job(oracle, bs), batchsize=bs) == 0
+    total, counts = W.workdir_sum(str(tmp_path))
+    assert counts == [d // bs + 1] * 7
+    assert total == oracle.to_hex(oracle.result(d, 0, 3), 3) == load_golden("oracle_small.json")["100000"]["hex192"]
+
+
+def test_skip_past_d(cbl, oracle):
+    fn = oracle_job(oracle, 1000)
+    d, _ = oracle.pos_to_d(10000)
+    assert fn(10000, 0, d // 1000 + 1, 1000) is None
+
+
+def test_shard_covers_disjointly():
+    from clbellard_gb300 import workmode as W
+    jobs = W.all_jobs(10 ** 6, 1000)
+    parts = [W.shard(jobs, r, 3) for r in range(3)]
+    assert sorted(j for p in parts for j in p) == sorted(jobs)
+    assert sum(len(p) for p in parts) == len(jobs)
+
+
+def _rank_main(rank, world, port, needD, bs, out_q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from oracle import oracle
+        from clbellard_gb300 import workmode as W
+        d, _ = oracle.pos_to_d(needD)
+        fn = oracle_job(oracle, bs)
+        mine = [fn(needD, s, b, bs) for s, b in W.shard(W.all_jobs(d, bs), rank, world)]
+        total = W.distributed_sum([h for h in mine if h is not None])
+        out_q.put((rank, total))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_rank_gloo_merge(oracle):
+    """Two CPU ranks shard the jobs, exchange 48-hex partials (the only
+    exchange step) and both obtain the single-process result."""
+    import multiprocessing as mp
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    needD, bs = 10000, 997
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, needD, bs, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    d, _ = oracle.pos_to_d(needD)
+    want = oracle.to_hex(oracle.result(d, 0, 3), 3)
+    assert res[0] == res[1] == want
