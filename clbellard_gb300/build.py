@@ -21,7 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
-UNITS = ["cbl_kernels.cu", "cbl_host.cu"]
+UNITS = ["cbl_kernels.cu", "cbl_host.cu", "cbl_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -306,6 +306,7 @@ const char *cbl_strerror(int code)
     case CBL_E_PRECISION: return "call not valid for this precision";
     case CBL_E_IO: return "file I/O error";
     case CBL_E_FORMAT: return "malformed input";
+    case CBL_E_LIMIT: return "request exceeds a fixed limit (at most CBL_NOALLOC_MAX_POSITIONS positions)";
     default: return "unknown error";
     }
 }

@@ -48,6 +48,7 @@ extern "C" {
 #define CBL_E_PRECISION  -8   /* call not valid for the context's precision */
 #define CBL_E_IO         -9   /* file read/write failed */
 #define CBL_E_FORMAT    -10   /* malformed hex string / worklist */
+#define CBL_E_LIMIT     -11   /* request larger than a fixed limit (cbl_batch_noalloc) */
 
 typedef struct cbl_ctx cbl_ctx;
 
@@ -154,6 +155,31 @@ int64_t cbl_launch_count(const cbl_ctx *ctx);
 /* Tuning: terms per warp tile (multiple of 32) and persistent CTAs per SM (0 = auto). */
 int cbl_set_tuning(cbl_ctx *ctx, int tile_terms, int ctas_per_sm);
 const char *cbl_strerror(int code);
+
+/* ---- allocation-free evaluation (no counterpart in the reference)
+ * For callers that must not allocate GPU memory themselves: programs whose
+ * device memory is owned by another allocator or fixed budget (a framework's
+ * caching allocator, a long-running service that allocates only at start-up),
+ * or pipelines that cannot absorb the device-wide synchronisation that
+ * cudaMalloc / cudaFree may cause. cbl_batch_noalloc evaluates up to
+ * CBL_NOALLOC_MAX_POSITIONS reference positions in 192-bit mode on the CURRENT
+ * device and stream and calls no cudaMalloc, cudaFree or other allocating
+ * routine. The caller passes pos[0..n) (host) and d_out3n, a device buffer it
+ * owns of 3*n uint64_t; d_out3n[3i..3i+2] receives position i's result (most
+ * significant word first), as cbl_batch, once `stream` (a cudaStream_t, 0 for
+ * the legacy default stream) reaches that point; the call itself returns
+ * without waiting.
+ * The kernels' scratch is one static device array of CBL_NOALLOC_SCRATCH_BYTES
+ * (about 106 KiB) that every GPU loading this library holds until the process
+ * exits. The first call on each device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before
+ * any stream capture. All calls on a device share the array and each call
+ * clears it before use, so calls whose work overlaps on the GPU (different
+ * streams, or several host threads) race and corrupt each other's results:
+ * serialise them. n > CBL_NOALLOC_MAX_POSITIONS returns CBL_E_LIMIT. */
+#define CBL_NOALLOC_MAX_POSITIONS 64
+#define CBL_NOALLOC_SCRATCH_BYTES 108032
+int cbl_batch_noalloc(const uint64_t *pos, int n, uint64_t *d_out3n, void *stream);
 
 /* ---- HSP-friendly variants: 64-bit arguments by pointer (HSP passes int64 vars
  * by address; #uselib/#func cannot pass 64-bit values directly). */
