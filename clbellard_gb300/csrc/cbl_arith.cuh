@@ -14,11 +14,12 @@
 // (exact division by the odd m), so q_j is the Montgomery multiplier of the
 // step and no division is ever executed. The chain ends at r_0 = 2^(10e) mod m.
 //
-// Two residue widths:
+// Three residue kinds:
 //   width 1 (m < 2^28): R = 2^32, residues kept lazily in [0, 4m).
+//   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m).
 //   width 2 (2^28 <= m < 2^50): R = 2^64 by two word steps, residues in [0, 4m).
-// The ladder step is y <- REDC(y^2) << b with b the next exponent bit; because
-// 16m < R the result stays below 4m with no conditional subtraction.
+// The ladder step is y <- REDC(y^2) << b with b the next exponent bit; in the
+// lazy kinds 16m < R keeps the result below 4m with no conditional subtraction.
 #pragma once
 #include <stdint.h>
 #include "cbl_internal.h"
@@ -43,22 +44,82 @@ __device__ __forceinline__ float rcp_approx(float x)
     return r;
 }
 
-// A value congruent to 2^E0 mod m in [0, 2m), for E0 = 33 (m < 2^28) or
-// E0 = 65 (2^28 <= m < 2^50). Two float-reciprocal quotient estimates:
-//   q1 = trunc(2^E0 / m) +- (2^(E0-21)/m + 1), so |r1| = |2^E0 - q1 m| <= 2^(E0-21) + m;
-//   q2 = rint(r1 / m) is then off by less than 1 (|r1/m| <= 2^16 + 1 in both
-//   uses), so r1 - q2 m lies in (-m, m) and adding m lands in (0, 2m).
-template <int E0>
-__device__ __forceinline__ uint64_t pow2_start(uint64_t m)
+// ------------------------------------------------------------ start values --
+// The ladder starts from a value congruent to 2^(Rb+1) (the exponent's leading
+// one already consumed). Two float-reciprocal quotient estimates with 32-bit
+// conversions only: q1 = trunc(2^E0 / m) is off by at most 2^(E0-21)/m + 1, so
+// r1 = 2^E0 - q1 m is small; q2 = rint(r1 / m) is then off by less than 1 and
+// r1 - q2 m lies in (-m, m).
+
+// trunc(x) for a positive float x < 2^63, as a 64-bit integer, from its bits.
+__device__ __forceinline__ uint64_t float_to_u64_trunc(float x)
 {
-    const float fm = __ull2float_rn(m);
+    const uint32_t bits = __float_as_uint(x);
+    const int e = (int)((bits >> 23) & 0xffu) - 127;
+    const uint64_t mant = (uint64_t)((bits & 0x7fffffu) | 0x800000u);
+    return e >= 23 ? (mant << (e - 23)) : (mant >> (23 - e));
+}
+
+// Width 1 (3 <= m < 2^28): a value in (0, 2m) congruent to 2^33.
+__device__ __forceinline__ uint32_t w1_start(uint32_t m)
+{
+    const float inv = rcp_approx(__uint2float_rn(m));
+    const uint32_t q1 = __float2uint_rz(8589934592.0f * inv);          // < 2^32 for m >= 3
+    const int32_t r1 = (int32_t)(0u - q1 * m);                          // 2^33 - q1 m, |r1| < 2^29
+    const int32_t q2 = __float2int_rn(__int2float_rn(r1) * inv);
+    return (uint32_t)(r1 + (1 - q2) * (int32_t)m);
+}
+
+// Strict width 1 (2^28 <= m < 2^32): 2^33 mod m in [0, m). q1 <= 32 is off by
+// at most one, so one correction either way suffices.
+__device__ __forceinline__ uint32_t w1s_start(uint32_t m)
+{
+    const float inv = rcp_approx(__uint2float_rn(m));
+    const uint32_t q1 = __float2uint_rz(8589934592.0f * inv);
+    int64_t r = (int64_t)(1ull << 33) - (int64_t)q1 * (int64_t)m;       // in [-m, 2m)
+    r += (r < 0) ? (int64_t)m : 0;
+    r -= (r >= (int64_t)m) ? (int64_t)m : 0;
+    return (uint32_t)r;
+}
+
+// Width 2 (2^28 <= m < 2^50): a value in (0, 2m) congruent to 2^65.
+__device__ __forceinline__ uint64_t w2_start(uint64_t m)
+{
+    const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
+    const float fm = __fmaf_rn(__uint2float_rn(m1), 4294967296.0f, __uint2float_rn(m0));
     const float inv = rcp_approx(fm);
-    const float scale = __int_as_float((127 + E0) << 23);         // 2^E0
-    const uint64_t q1 = __float2ull_rz(scale * inv);
-    const uint64_t top = (E0 < 64) ? (1ull << (E0 & 63)) : 0ull;  // 2^E0 mod 2^64
-    const int64_t r1 = (int64_t)(top - q1 * m);
-    const int64_t q2 = __float2ll_rn(__ll2float_rn(r1) * inv);
-    return (uint64_t)(r1 - (q2 - 1) * (int64_t)m);
+    const uint64_t q1 = float_to_u64_trunc(36893488147419103232.0f * inv);   // 2^65 / m
+    const int64_t r1 = (int64_t)(0ull - q1 * m);                               // |r1| <= 2^44 + m
+    const float fr1 = __fmaf_rn(__int2float_rn((int32_t)(r1 >> 32)), 4294967296.0f,
+                                __uint2float_rn((uint32_t)r1));
+    const int32_t q2 = __float2int_rn(fr1 * inv);                             // |r1/m| <= 2^16 + 1
+    return (uint64_t)(r1 + (int64_t)(1 - q2) * (int64_t)m);
+}
+
+// ------------------------------------------------------------ exponent walk --
+// Calls st.step(b) for every bit of Ep after its leading one, most significant
+// first. When Ep >= 2^32 the 32 bits of the low word run fully unrolled.
+template <typename State>
+__device__ __forceinline__ void walk_bits(uint64_t Ep, State &st)
+{
+    const uint32_t hi = (uint32_t)(Ep >> 32), lo = (uint32_t)Ep;
+    if (hi != 0) {
+        const int nb = 32 - __clz(hi);
+        uint32_t h = (hi << (32 - nb)) << 1;
+        for (int i = 1; i < nb; ++i) {
+            st.step(h >> 31);
+            h <<= 1;
+        }
+#pragma unroll
+        for (int i = 31; i >= 0; --i) st.step((lo >> i) & 1u);
+    } else {
+        const int nb = 32 - __clz(lo);
+        uint32_t l = (lo << (32 - nb)) << 1;
+        for (int i = 1; i < nb; ++i) {
+            st.step(l >> 31);
+            l <<= 1;
+        }
+    }
 }
 
 // ---------------------------------------------------------------- width 1 --
@@ -71,26 +132,24 @@ __device__ __forceinline__ uint32_t w1_sqr(uint32_t y, uint32_t m, uint32_t mp, 
     return (uint32_t)(s >> 32) << b;
 }
 
+struct W1State {
+    uint32_t y, m, mp;
+    __device__ __forceinline__ void step(uint32_t b) { y = w1_sqr(y, m, mp, b); }
+};
+
 // r6 = 2^E mod m in [0, m) for E >= 33 (m < 2^28, odd, >= 3).
 __device__ __forceinline__ uint32_t w1_pow2(uint64_t E, uint32_t m, uint32_t mp)
 {
-    // Ladder on E' = E - 32: invariant y = 2^(32 + prefix of E').
-    const uint64_t Ep = E - 32;
-    const int nb = 64 - __clzll((long long)Ep);
-    uint64_t bits = Ep << (64 - nb);                    // leading 1 at bit 63
-    uint32_t y = (uint32_t)pow2_start<33>(m);           // prefix '1': 2^33
-    bits <<= 1;
-    for (int i = 1; i < nb; ++i) {
-        const uint32_t b = (uint32_t)(bits >> 63);
-        bits <<= 1;
-        y = w1_sqr(y, m, mp, b);
-    }
+    W1State st{w1_start(m), m, mp};                     // invariant y = 2^(32 + prefix of E - 32)
+    walk_bits(E - 32, st);
+    uint32_t y = st.y;
     y = min(y, y - 2u * m);                            // [0,4m) -> [0,2m)
     y = min(y, y - m);                                 //        -> [0,m)
     return y;
 }
 
 // Six quotient digits of r_0 / m from r6 (digit 0 least significant), and r_0.
+// Valid for any odd m < 2^32.
 __device__ __forceinline__ uint32_t w1_digits(uint32_t r, uint32_t m, uint32_t mp, uint32_t q[6])
 {
 #pragma unroll
@@ -99,6 +158,54 @@ __device__ __forceinline__ uint32_t w1_digits(uint32_t r, uint32_t m, uint32_t m
         r = (uint32_t)(((uint64_t)q[j] * m + r) >> 32);
     }
     return r;
+}
+
+// --------------------------------------------------------- strict width 1 --
+// 2^28 <= m < 2^32: R = 2^32 with residues in [0, m). REDC(y^2) < 2m needs one
+// conditional subtraction (with the carry out of bit 32), and so does 2y.
+__device__ __forceinline__ uint32_t w1s_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
+{
+    const uint64_t t = (uint64_t)y * y;
+    const uint32_t t0 = (uint32_t)t, t1 = (uint32_t)(t >> 32);
+    const uint32_t u = t0 * mp;
+    const uint64_t v = (uint64_t)u * m;
+    uint32_t z, c;
+    asm("add.cc.u32 %0, %2, %3;\n\t"                   // carry = (t0 != 0): t0 + lo(um) = 0 mod 2^32
+        "addc.cc.u32 %0, %4, %5;\n\t"
+        "addc.u32 %1, 0, 0;"
+        : "=r"(z), "=r"(c)
+        : "r"(t0), "r"((uint32_t)v), "r"(t1), "r"((uint32_t)(v >> 32)));
+    uint32_t zm, bw;                                    // (c:z) - m, borrow-extended
+    asm("sub.cc.u32 %0, %2, %3;\n\t"
+        "subc.u32 %1, %4, 0;"
+        : "=r"(zm), "=r"(bw)
+        : "r"(z), "r"(m), "r"(c));
+    z = bw ? z : zm;
+    const uint32_t dd = z & (0u - b);                   // doubling when b
+    uint32_t z2, c2;
+    asm("add.cc.u32 %0, %2, %3;\n\t"
+        "addc.u32 %1, 0, 0;"
+        : "=r"(z2), "=r"(c2)
+        : "r"(z), "r"(dd));
+    uint32_t z2m, bw2;
+    asm("sub.cc.u32 %0, %2, %3;\n\t"
+        "subc.u32 %1, %4, 0;"
+        : "=r"(z2m), "=r"(bw2)
+        : "r"(z2), "r"(m), "r"(c2));
+    return bw2 ? z2 : z2m;
+}
+
+struct W1SState {
+    uint32_t y, m, mp;
+    __device__ __forceinline__ void step(uint32_t b) { y = w1s_sqr(y, m, mp, b); }
+};
+
+// r6 = 2^E mod m in [0, m) for E >= 33 (2^28 <= m < 2^32).
+__device__ __forceinline__ uint32_t w1s_pow2(uint64_t E, uint32_t m, uint32_t mp)
+{
+    W1SState st{w1s_start(m), m, mp};
+    walk_bits(E - 32, st);
+    return st.y;
 }
 
 // ---------------------------------------------------------------- width 2 --
@@ -138,22 +245,18 @@ __device__ __forceinline__ void w2_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0, 
     y0 = z0 << b;
 }
 
-// r6 = 2^E mod m in [0, m) as (lo, hi) for E >= 65 (2^28 <= m < 2^50).
+struct W2State {
+    uint32_t y0, y1, m0, m1, mp;
+    __device__ __forceinline__ void step(uint32_t b) { w2_sqr(y0, y1, m0, m1, mp, b); }
+};
+
+// r6 = 2^E mod m in [0, m) for E >= 65 (2^28 <= m < 2^50).
 __device__ __forceinline__ uint64_t w2_pow2(uint64_t E, uint64_t m, uint32_t mp)
 {
-    const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
-    const uint64_t Ep = E - 64;
-    const int nb = 64 - __clzll((long long)Ep);
-    uint64_t bits = Ep << (64 - nb);
-    const uint64_t y = pow2_start<65>(m);               // prefix '1': 2^65
-    uint32_t y0 = (uint32_t)y, y1 = (uint32_t)(y >> 32);
-    bits <<= 1;
-    for (int i = 1; i < nb; ++i) {
-        const uint32_t b = (uint32_t)(bits >> 63);
-        bits <<= 1;
-        w2_sqr(y0, y1, m0, m1, mp, b);
-    }
-    uint64_t r = ((uint64_t)y1 << 32) | y0;
+    const uint64_t y = w2_start(m);
+    W2State st{(uint32_t)y, (uint32_t)(y >> 32), (uint32_t)m, (uint32_t)(m >> 32), mp};
+    walk_bits(E - 64, st);
+    uint64_t r = ((uint64_t)st.y1 << 32) | st.y0;
     r = min(r, r - 2 * m);
     r = min(r, r - m);
     return r;

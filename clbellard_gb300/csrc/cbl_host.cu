@@ -135,17 +135,18 @@ bool series_ok(uint64_t den0, uint64_t den1)
 }
 
 // Append the segments covering k in [k0, k1) of one series, split at d (main
-// vs tail) and at the width boundary m = 2^28. k = 0 with den1 = 1 (m = 1)
-// contributes exactly 0 and is left out.
+// vs tail) and at the residue-kind boundaries m = 2^28 and m = 2^32. k = 0 with
+// den1 = 1 (m = 1) contributes exactly 0 and is left out.
 int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, int sign, uint32_t slot,
                  uint64_t k0, uint64_t k1)
 {
     if (k0 == 0 && den1 == 1) k0 = 1;
     if (k1 <= k0) return CBL_OK;
     if ((u128)den0 * (k1 - 1) + den1 >= (u128)kW2Max) return CBL_E_POSITION;
-    const uint64_t kw = (kW1Max - den1 + den0 - 1) / den0;   // first k with m >= 2^28
-    const uint64_t cuts[2] = {std::min(std::max(d, k0), k1), std::min(std::max(kw, k0), k1)};
-    std::vector<uint64_t> pts = {k0, cuts[0], cuts[1], k1};
+    const uint64_t kw1 = (kW1Max - den1 + den0 - 1) / den0;    // first k with m >= 2^28
+    const uint64_t kw1s = (kW1SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^32
+    std::vector<uint64_t> pts = {k0, k1};
+    for (uint64_t c : {d, kw1, kw1s}) pts.push_back(std::min(std::max(c, k0), k1));
     std::sort(pts.begin(), pts.end());
     for (size_t i = 0; i + 1 < pts.size(); ++i) {
         const uint64_t a = pts[i], b = pts[i + 1];
@@ -157,10 +158,17 @@ int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, 
         s.den0 = den0;
         s.den1 = den1;
         s.slot = slot;
-        s.flags = seg_flags(sign, a >= kw ? 2 : 1);
+        s.flags = seg_flags(sign, a >= kw1s ? 2 : (a >= kw1 ? 3 : 1));
         v.push_back(s);
     }
     return CBL_OK;
+}
+
+// Cost rank of a residue kind: width 2 > strict width 1 > width 1.
+int kind_rank(uint32_t flags)
+{
+    const uint32_t k = (flags >> 4) & 15u;
+    return k == 2 ? 2 : (k == 3 ? 1 : 0);
 }
 
 // Costlier tiles first (width 2, then large d), tails last; then tile prefixes.
@@ -169,8 +177,8 @@ uint64_t order_and_number(std::vector<Seg> &v, uint32_t tile_k)
     std::stable_sort(v.begin(), v.end(), [](const Seg &a, const Seg &b) {
         const bool ta = a.k0 >= a.d, tb = b.k0 >= b.d;
         if (ta != tb) return !ta;
-        const uint32_t wa = (a.flags >> 4) & 15u, wb = (b.flags >> 4) & 15u;
-        if (wa != wb) return wa > wb;
+        const int ra = kind_rank(a.flags), rb = kind_rank(b.flags);
+        if (ra != rb) return ra > rb;
         return a.d > b.d;
     });
     uint64_t t = 0;
@@ -902,7 +910,7 @@ int cbl_probe_imad(cbl_ctx *c, int iters, double *ops_per_s, double *ms)
     if (!c || iters <= 0) return CBL_E_ARG;
     cudaSetDevice(c->device);
     uint32_t *d_sink = nullptr;
-    const int grid = c->sm_count * 8, block = 256;
+    const int grid = probe_imad_grid(c->sm_count), block = 256;
     if (cudaMalloc(&d_sink, sizeof(uint32_t) * grid * block) != cudaSuccess) return CBL_E_NOMEM;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);

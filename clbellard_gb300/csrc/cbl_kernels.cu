@@ -48,13 +48,18 @@ __device__ __forceinline__ void shr192(uint32_t q[6], int s)
 
 // One term's six quotient digits: k < d gives frac(2^(10(d-k))/m), k >= d the
 // tail value 2^(-10(k-d))/m (digits of 1/m shifted right by 10(k-d)).
-template <int WIDTH, bool TAIL>
+// KIND: 1 = width 1 (m < 2^28), 3 = strict width 1 (2^28 <= m < 2^32),
+// 2 = width 2 (2^28 <= m < 2^50).
+template <int KIND, bool TAIL>
 __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, uint32_t q[6])
 {
     const uint32_t mp = neg_inv32((uint32_t)m);
     const uint64_t E = TAIL ? 192ull : 10ull * (d - k) + 192ull;
-    if (WIDTH == 1) {
+    if (KIND == 1) {
         const uint32_t r6 = w1_pow2(E, (uint32_t)m, mp);
+        w1_digits(r6, (uint32_t)m, mp, q);
+    } else if (KIND == 3) {
+        const uint32_t r6 = w1s_pow2(E, (uint32_t)m, mp);
         w1_digits(r6, (uint32_t)m, mp, q);
     } else {
         const uint64_t r6 = w2_pow2(E, m, mp);
@@ -63,14 +68,14 @@ __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, 
     if (TAIL) shr192(q, (int)(10 * (k - d)));
 }
 
-template <int WIDTH, bool TAIL>
+template <int KIND, bool TAIL>
 __device__ __forceinline__ void run_tile(const Seg &s, uint64_t kb, uint64_t ke, int lane, Acc192 &acc,
                                          uint32_t &cnt)
 {
     for (uint64_t k = kb + lane; k < ke; k += 32) {
         const uint64_t m = (uint64_t)s.den0 * k + s.den1;
         uint32_t q[6];
-        term_digits<WIDTH, TAIL>(s.d, k, m, q);
+        term_digits<KIND, TAIL>(s.d, k, m, q);
         acc_add(acc, q);
         ++cnt;
     }
@@ -126,9 +131,11 @@ __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restri
         uint32_t cnt = 0;
         if (tail) {
             if (width == 1) run_tile<1, true>(s, kb, ke, lane, acc, cnt);
+            else if (width == 3) run_tile<3, true>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, true>(s, kb, ke, lane, acc, cnt);
         } else {
             if (width == 1) run_tile<1, false>(s, kb, ke, lane, acc, cnt);
+            else if (width == 3) run_tile<3, false>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, false>(s, kb, ke, lane, acc, cnt);
         }
         // Every k of this lane has the parity of kb + lane: sign (-1)^(k + sign).
@@ -268,9 +275,13 @@ __global__ void terms_each_kernel(uint64_t d, uint32_t den0, uint32_t den1, int 
     uint32_t q[6] = {0, 0, 0, 0, 0, 0};
     if (m != 1) {
         if (k < d) {
-            if (m < kW1Max) term_digits<1, false>(d, k, m, q); else term_digits<2, false>(d, k, m, q);
+            if (m < kW1Max) term_digits<1, false>(d, k, m, q);
+            else if (m < kW1SMax) term_digits<3, false>(d, k, m, q);
+            else term_digits<2, false>(d, k, m, q);
         } else {
-            if (m < kW1Max) term_digits<1, true>(d, k, m, q); else term_digits<2, true>(d, k, m, q);
+            if (m < kW1Max) term_digits<1, true>(d, k, m, q);
+            else if (m < kW1SMax) term_digits<3, true>(d, k, m, q);
+            else term_digits<2, true>(d, k, m, q);
         }
         if ((k + (uint64_t)sign) & 1ull)
             for (int j = 0; j < 6; ++j) q[j] = ~q[j];
@@ -356,6 +367,7 @@ __global__ void __launch_bounds__(kBlockDD) dd_terms_kernel(double2 *bigsum, uin
         uint32_t q[6];
         uint64_t r;
         if (m < kW1Max) r = w1_digits(w1_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
+        else if (m < kW1SMax) r = w1_digits(w1s_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
         else r = w2_digits(w2_pow2(E, m, mp), m, mp, q);
         DD t = dd_div_nn((double)r, (double)m);
         if ((k + (uint64_t)sign) & 1ull) { t.hi = -t.hi; t.lo = -t.lo; }
@@ -448,36 +460,46 @@ cudaError_t launch_dd_sum7(double2 *partial, double2 *ans, int numer, cudaStream
 namespace cbl {
 
 // ------------------------------------------------------------ IMAD probe --
-// 16 independent multiply chains per thread (8 mad.lo.u32, 8 mad.hi.u32):
-// the issue rate of 32-bit multiply halves, the unit of the term kernels'
-// algorithmic work.
+// 16 independent mad.wide.u32 chains per thread: each instruction forms both
+// 32-bit halves of a 32x32 product, the most multiply halves per issue this
+// GPU offers (mad.lo.u32 issues at the same rate with one half, mad.hi.u32 at
+// half that rate). The issue rate x 2 is the peak of the term kernels'
+// algorithmic work unit.
 __global__ void __launch_bounds__(256) probe_imad_kernel(uint32_t *sink, int iters)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t a[8], b[8];
+    uint64_t w[16];
+    uint32_t a[16];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        a[j] = t * 2654435761u + j;
-        b[j] = t ^ (0x9e3779b9u * (j + 1));
+    for (int j = 0; j < 16; ++j) {
+        a[j] = t * 2654435761u + 7919u * j;
+        w[j] = t ^ (0x9e3779b9u * (j + 1));
     }
-    const uint32_t k1 = 0x7feb352du | 1u, k2 = 0x846ca68bu;
+    const uint32_t k1 = 0x7feb352du;
+    // 16 independent accumulator chains; the multiplicands do not depend on them,
+    // so the issue rate (not the latency) of mad.wide is measured
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[j]) : "r"(k1), "r"(b[j]));
-            asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(b[j]) : "r"(k2), "r"(a[j]));
-        }
+        for (int j = 0; j < 16; ++j) asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(w[j]) : "r"(a[j]), "r"(k1));
     }
     uint32_t x = 0;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) x ^= a[j] ^ b[j];
+    for (int j = 0; j < 16; ++j) x ^= (uint32_t)w[j] ^ (uint32_t)(w[j] >> 32);
     sink[t] = x;
+}
+
+int probe_imad_grid(int sm_count)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, probe_imad_kernel, 256, 0) != cudaSuccess || n < 1) n = 1;
+    return sm_count * n;
 }
 
 cudaError_t launch_probe_imad(uint32_t *sink, int grid, int block, int iters, uint64_t *ops, cudaStream_t st)
 {
-    probe_imad_kernel<<<grid, block, 0, st>>>(sink, iters);
-    if (ops) *ops = (uint64_t)grid * block * (uint64_t)iters * 16ull;
+    (void)block;
+    probe_imad_kernel<<<grid, 256, 0, st>>>(sink, iters);
+    if (ops) *ops = (uint64_t)grid * block * (uint64_t)iters * 16ull * 2ull;   // two halves per mad.wide
     return cudaGetLastError();
 }
 
