@@ -14,9 +14,10 @@
 // (exact division by the odd m), so q_j is the Montgomery multiplier of the
 // step and no division is ever executed. The chain ends at r_0 = 2^(10e) mod m.
 //
-// Three residue kinds:
+// Four residue kinds:
 //   width 1 (m < 2^28): R = 2^32, residues kept lazily in [0, 4m).
 //   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m).
+//   short width 2 (2^32 <= m < 2^40): R = 2^64, residues in [0, 4m).
 //   width 2 (2^28 <= m < 2^50): R = 2^64 by two word steps, residues in [0, 4m).
 // The ladder step is y <- REDC(y^2) << b with b the next exponent bit; in the
 // lazy kinds 16m < R keeps the result below 4m with no conditional subtraction.
@@ -256,6 +257,101 @@ __device__ __forceinline__ uint64_t w2_pow2(uint64_t E, uint64_t m, uint32_t mp)
     const uint64_t y = w2_start(m);
     W2State st{(uint32_t)y, (uint32_t)(y >> 32), (uint32_t)m, (uint32_t)(m >> 32), mp};
     walk_bits(E - 64, st);
+    uint64_t r = ((uint64_t)st.y1 << 32) | st.y0;
+    r = min(r, r - 2 * m);
+    r = min(r, r - m);
+    return r;
+}
+
+// --------------------------------------------------- width 2, m < 2^40 --
+// 2^32 <= m < 2^40 (m1 < 2^8), y in [0,4m) (y1 < 2^10). Same REDC_2^64 as
+// w2_sqr, arranged so that every multiply-add takes a full product as its
+// 64-bit addend: u0 m0 + y0^2 and u1 m0 + s wrap past 2^64 at most once and the
+// lost carry is recovered by an unsigned compare of the high words.
+__device__ __forceinline__ void w2s_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0, uint32_t m1, uint32_t mp,
+                                        uint32_t b)
+{
+    const uint64_t A = (uint64_t)y0 * y0;
+    const uint64_t P = (uint64_t)y0 * (y1 << 1);               // 2 y0 y1 < 2^43
+    const uint32_t a0 = (uint32_t)A, a1 = (uint32_t)(A >> 32);
+    const uint32_t u0 = a0 * mp;
+    const uint64_t X = (uint64_t)u0 * m0 + A;                 // low word 0; = (a1 + h0) 2^32 mod 2^64
+    const uint32_t x1 = (uint32_t)(X >> 32);
+    const uint32_t w = y1 * y1 + (x1 < a1 ? 1u : 0u);          // y1^2 < 2^20 plus the wrapped carry
+    const uint64_t Q = (uint64_t)u0 * m1 + P;                 // < 2^44
+    uint32_t s0, s1;                                           // s = (T + u0 m) / 2^32 < 2^54
+    asm("add.cc.u32 %0, %2, %3;\n\t"
+        "addc.u32 %1, %4, %5;"
+        : "=r"(s0), "=r"(s1)
+        : "r"((uint32_t)Q), "r"(x1), "r"((uint32_t)(Q >> 32)), "r"(w));
+    const uint64_t s = ((uint64_t)s1 << 32) | s0;
+    const uint32_t u1 = s0 * mp;
+    const uint64_t Y = (uint64_t)u1 * m0 + s;                 // low word 0; = (s1 + h1) 2^32 mod 2^64
+    const uint32_t yw = (uint32_t)(Y >> 32);
+    const uint32_t c2 = yw < s1 ? 1u : 0u;
+    const uint64_t Zq = (uint64_t)u1 * m1;                    // < 2^40
+    uint32_t z0, z1;                                           // z = (s + u1 m) / 2^32 < 2m
+    asm("add.cc.u32 %0, %2, %3;\n\t"
+        "addc.u32 %1, %4, %5;"
+        : "=r"(z0), "=r"(z1)
+        : "r"((uint32_t)Zq), "r"(yw), "r"((uint32_t)(Zq >> 32)), "r"(c2));
+    y1 = __funnelshift_l(z0, z1, b);
+    y0 = z0 << b;
+}
+
+struct W2SState {
+    uint32_t y0, y1, m0, m1, mp;
+    __device__ __forceinline__ void step(uint32_t b) { w2s_sqr(y0, y1, m0, m1, mp, b); }
+};
+
+// A value in (0, 2m) congruent to 2^(64 + p), 1 <= p <= 7, for 2^32 <= m < 2^40:
+// |2^(64+p) - q1 m| <= 2^(43+p) + m and |r1/m| <= 2^18, so two rounds suffice.
+__device__ __forceinline__ uint64_t w2s_start(uint64_t m, uint32_t p)
+{
+    const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
+    const float fm = __fmaf_rn(__uint2float_rn(m1), 4294967296.0f, __uint2float_rn(m0));
+    const float inv = rcp_approx(fm);
+    const float scale = __int_as_float((int)((127u + 64u + p) << 23));      // 2^(64+p)
+    const uint64_t q1 = float_to_u64_trunc(scale * inv);
+    const int64_t r1 = (int64_t)(0ull - q1 * m);
+    const float fr1 = __fmaf_rn(__int2float_rn((int32_t)(r1 >> 32)), 4294967296.0f,
+                                __uint2float_rn((uint32_t)r1));
+    const int32_t q2 = __float2int_rn(fr1 * inv);
+    return (uint64_t)(r1 + (int64_t)(1 - q2) * (int64_t)m);
+}
+
+// r6 = 2^E mod m in [0, m) for E >= 65, 2^32 <= m < 2^40. The start value
+// takes the leading up-to-three bits of E - 64 at once.
+__device__ __forceinline__ uint64_t w2s_pow2(uint64_t E, uint64_t m, uint32_t mp)
+{
+    const uint64_t Ep = E - 64;
+    const uint32_t hi = (uint32_t)(Ep >> 32), lo = (uint32_t)Ep;
+    W2SState st{0, 0, (uint32_t)m, (uint32_t)(m >> 32), mp};
+    if (hi != 0) {
+        const int nb = 32 - __clz(hi);
+        const int t = nb < 3 ? nb : 3;
+        const uint64_t y = w2s_start(m, hi >> (nb - t));
+        st.y0 = (uint32_t)y;
+        st.y1 = (uint32_t)(y >> 32);
+        uint32_t h = (nb - t) > 0 ? hi << (32 - (nb - t)) : 0u;   // remaining bits of hi, left-aligned
+        for (int i = t; i < nb; ++i) {
+            st.step(h >> 31);
+            h <<= 1;
+        }
+#pragma unroll
+        for (int i = 31; i >= 0; --i) st.step((lo >> i) & 1u);
+    } else {
+        const int nb = 32 - __clz(lo);
+        const int t = nb < 3 ? nb : 3;
+        const uint64_t y = w2s_start(m, lo >> (nb - t));
+        st.y0 = (uint32_t)y;
+        st.y1 = (uint32_t)(y >> 32);
+        uint32_t l = (nb - t) > 0 ? lo << (32 - (nb - t)) : 0u;
+        for (int i = t; i < nb; ++i) {
+            st.step(l >> 31);
+            l <<= 1;
+        }
+    }
     uint64_t r = ((uint64_t)st.y1 << 32) | st.y0;
     r = min(r, r - 2 * m);
     r = min(r, r - m);

@@ -135,7 +135,7 @@ bool series_ok(uint64_t den0, uint64_t den1)
 }
 
 // Append the segments covering k in [k0, k1) of one series, split at d (main
-// vs tail) and at the residue-kind boundaries m = 2^28 and m = 2^32. k = 0 with
+// vs tail) and at the residue-kind boundaries m = 2^28, 2^32 and 2^40. k = 0 with
 // den1 = 1 (m = 1) contributes exactly 0 and is left out.
 int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, int sign, uint32_t slot,
                  uint64_t k0, uint64_t k1)
@@ -145,8 +145,9 @@ int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, 
     if ((u128)den0 * (k1 - 1) + den1 >= (u128)kW2Max) return CBL_E_POSITION;
     const uint64_t kw1 = (kW1Max - den1 + den0 - 1) / den0;    // first k with m >= 2^28
     const uint64_t kw1s = (kW1SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^32
+    const uint64_t kw2s = (kW2SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^40
     std::vector<uint64_t> pts = {k0, k1};
-    for (uint64_t c : {d, kw1, kw1s}) pts.push_back(std::min(std::max(c, k0), k1));
+    for (uint64_t c : {d, kw1, kw1s, kw2s}) pts.push_back(std::min(std::max(c, k0), k1));
     std::sort(pts.begin(), pts.end());
     for (size_t i = 0; i + 1 < pts.size(); ++i) {
         const uint64_t a = pts[i], b = pts[i + 1];
@@ -158,17 +159,17 @@ int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, 
         s.den0 = den0;
         s.den1 = den1;
         s.slot = slot;
-        s.flags = seg_flags(sign, a >= kw1s ? 2 : (a >= kw1 ? 3 : 1));
+        s.flags = seg_flags(sign, a >= kw2s ? 2 : (a >= kw1s ? 4 : (a >= kw1 ? 3 : 1)));
         v.push_back(s);
     }
     return CBL_OK;
 }
 
-// Cost rank of a residue kind: width 2 > strict width 1 > width 1.
+// Cost rank of a residue kind: width 2 > short width 2 > strict width 1 > width 1.
 int kind_rank(uint32_t flags)
 {
     const uint32_t k = (flags >> 4) & 15u;
-    return k == 2 ? 2 : (k == 3 ? 1 : 0);
+    return k == 2 ? 3 : (k == 4 ? 2 : (k == 3 ? 1 : 0));
 }
 
 // Costlier tiles first (width 2, then large d), tails last; then tile prefixes.

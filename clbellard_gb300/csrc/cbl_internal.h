@@ -16,6 +16,7 @@ constexpr uint32_t kDen1[7] = {1, 3, 1, 3, 5, 7, 9};
 // Residue-width limits of the term kernels (m odd, m >= 3).
 constexpr uint64_t kW1Max = 1ull << 28;   // width 1 (one 32-bit word) for m < 2^28
 constexpr uint64_t kW1SMax = 1ull << 32;  // strict width 1 for 2^28 <= m < 2^32
+constexpr uint64_t kW2SMax = 1ull << 40;  // short width 2 for 2^32 <= m < 2^40
 constexpr uint64_t kW2Max = 1ull << 50;   // width 2 (two words) for m < 2^50
 
 constexpr int kTail192 = 20;   // tail terms k = d..d+19 (Bellard.cl:1164-1239)
@@ -30,7 +31,7 @@ struct Seg {
     uint64_t tile0;
     uint32_t den0, den1;
     uint32_t slot;         // accumulator slot (6 x u64 digit sums)
-    uint32_t flags;        // bit 0: series sign (1 = minus), bits 4-7: residue kind 1|2|3
+    uint32_t flags;        // bit 0: series sign (1 = minus), bits 4-7: residue kind 1|2|3|4
 };
 static_assert(sizeof(Seg) == 48, "Seg layout");
 

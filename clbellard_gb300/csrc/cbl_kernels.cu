@@ -49,7 +49,7 @@ __device__ __forceinline__ void shr192(uint32_t q[6], int s)
 // One term's six quotient digits: k < d gives frac(2^(10(d-k))/m), k >= d the
 // tail value 2^(-10(k-d))/m (digits of 1/m shifted right by 10(k-d)).
 // KIND: 1 = width 1 (m < 2^28), 3 = strict width 1 (2^28 <= m < 2^32),
-// 2 = width 2 (2^28 <= m < 2^50).
+// 4 = short width 2 (2^32 <= m < 2^40), 2 = width 2 (2^28 <= m < 2^50).
 template <int KIND, bool TAIL>
 __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, uint32_t q[6])
 {
@@ -61,6 +61,9 @@ __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, 
     } else if (KIND == 3) {
         const uint32_t r6 = w1s_pow2(E, (uint32_t)m, mp);
         w1_digits(r6, (uint32_t)m, mp, q);
+    } else if (KIND == 4) {
+        const uint64_t r6 = w2s_pow2(E, m, mp);
+        w2_digits(r6, m, mp, q);
     } else {
         const uint64_t r6 = w2_pow2(E, m, mp);
         w2_digits(r6, m, mp, q);
@@ -132,10 +135,12 @@ __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restri
         if (tail) {
             if (width == 1) run_tile<1, true>(s, kb, ke, lane, acc, cnt);
             else if (width == 3) run_tile<3, true>(s, kb, ke, lane, acc, cnt);
+            else if (width == 4) run_tile<4, true>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, true>(s, kb, ke, lane, acc, cnt);
         } else {
             if (width == 1) run_tile<1, false>(s, kb, ke, lane, acc, cnt);
             else if (width == 3) run_tile<3, false>(s, kb, ke, lane, acc, cnt);
+            else if (width == 4) run_tile<4, false>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, false>(s, kb, ke, lane, acc, cnt);
         }
         // Every k of this lane has the parity of kb + lane: sign (-1)^(k + sign).
@@ -277,10 +282,12 @@ __global__ void terms_each_kernel(uint64_t d, uint32_t den0, uint32_t den1, int 
         if (k < d) {
             if (m < kW1Max) term_digits<1, false>(d, k, m, q);
             else if (m < kW1SMax) term_digits<3, false>(d, k, m, q);
+            else if (m < kW2SMax) term_digits<4, false>(d, k, m, q);
             else term_digits<2, false>(d, k, m, q);
         } else {
             if (m < kW1Max) term_digits<1, true>(d, k, m, q);
             else if (m < kW1SMax) term_digits<3, true>(d, k, m, q);
+            else if (m < kW2SMax) term_digits<4, true>(d, k, m, q);
             else term_digits<2, true>(d, k, m, q);
         }
         if ((k + (uint64_t)sign) & 1ull)
@@ -368,6 +375,7 @@ __global__ void __launch_bounds__(kBlockDD) dd_terms_kernel(double2 *bigsum, uin
         uint64_t r;
         if (m < kW1Max) r = w1_digits(w1_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
         else if (m < kW1SMax) r = w1_digits(w1s_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
+        else if (m < kW2SMax) r = w2_digits(w2s_pow2(E, m, mp), m, mp, q);
         else r = w2_digits(w2_pow2(E, m, mp), m, mp, q);
         DD t = dd_div_nn((double)r, (double)m);
         if ((k + (uint64_t)sign) & 1ull) { t.hi = -t.hi; t.lo = -t.lo; }

@@ -42,6 +42,15 @@ def test_terms_32bit_boundary(ctx192, oracle, f):
     check_terms(ctx192, oracle, d, f, list(range(k32 - 40, k32 + 40)))
 
 
+@pytest.mark.parametrize("f", range(7))
+def test_terms_40bit_boundary(ctx192, oracle, f):
+    """k around the first modulus >= 2^40 (short width 2 -> width 2)."""
+    den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
+    k40 = ((1 << 40) - den1 + den0 - 1) // den0
+    d = 399999999999
+    check_terms(ctx192, oracle, d, f, list(range(k40 - 40, k40 + 40)) + list(range(d - 40, d + 20)))
+
+
 def test_terms_sampled_1e8(ctx192, oracle):
     """1e5 seeded n at position 1e8 (all moduli < 2^32), all 7 series."""
     rng = random.Random(0x5EED)
