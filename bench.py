@@ -172,17 +172,38 @@ def max_over_ranks(x: float, world: int) -> float:
     return float(t.item())
 
 
+def reference_sample_rate(needD: int, target_s: float, threads: int):
+    """The reference's own kernels (oracle/_ref, compiled from its OpenCL
+    sources as C++; precision 2, the 192-bit integer mode) on a stratified
+    sample of the workload: per series, 8 k-ranges spread over [0, d)."""
+    from oracle.ref_harness import build as R
+    r = R.run(needD, 2, threads=threads, sample=(1 << 19, 8))
+    rate = r["terms_per_s"]
+    L = max(1 << 19, int(rate * target_s / 56))
+    r = R.run(needD, 2, threads=threads, sample=(L, 8))
+    return r["terms_per_s"], ("reference kernels (precision 2) on 7 series x 8 chunks of %d k spread over [0,d) "
+                              "at position %d" % (L, needD)), r.get("threads", threads)
+
+
 def reference_arm(args):
     world, rank, _ = dist_init()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     from oracle import oracle as O
+    from oracle.ref_harness import build as R
     d, _ = O.pos_to_d(POSITION)
+    use_ref = R.runnable()
     rates = []
     desc = ""
+    cores = threads
     for i in range(args.warmup + args.steps):
-        r, desc, cores = cpu_sample_rate(POSITION, args.ref_seconds, threads)
+        if use_ref:
+            r, desc, cores = reference_sample_rate(POSITION, args.ref_seconds, threads)
+        else:
+            r, desc, cores = cpu_sample_rate(POSITION, args.ref_seconds, threads)
+            desc += ("; the reference's OpenCL/HSP host cannot run here and its kernels were not compiled for "
+                     "this machine, so its CPU restatement (oracle/, Montgomery + exact long division) is timed")
         if i >= args.warmup:
             rates.append(r)
     value = statistics.median(rates)
@@ -192,9 +213,8 @@ def reference_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64 int", "data": "synthetic",
         "config": {"workload": "pi hex position 1e10, 192-bit fixed point, 7 series x d=%d terms" % d,
                    "position": POSITION, "d": d, "mode": "192-bit"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": desc + "; the reference's OpenCL/HSP host cannot run here, its CPU "
-                                          "restatement (oracle/, Montgomery + exact long division) is timed"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "reference" if use_ref else "port",
+                         "sample": desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -332,7 +352,7 @@ def main():
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dd", action="store_true", default=True)
     ap.add_argument("--no-dd", dest="dd", action="store_false")

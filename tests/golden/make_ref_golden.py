@@ -1,0 +1,52 @@
+"""Generate tests/golden/ref_outputs.json by running the reference's own
+kernels (compiled as C++ on the CPU by oracle/ref_harness) at several
+positions in all three precision modes. Needs the reference tree; the
+committed JSON is what the tests read.
+
+    python tests/golden/make_ref_golden.py [--big]
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+from fractions import Fraction
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.ref_harness import build as R  # noqa: E402
+
+POSITIONS = [1000, 10000, 100000, 1000000, 10000000]
+BIG = [100000000]
+
+
+def dd_hex(hi: float, lo: float) -> str:
+    """The exact value hi+lo in [0,1) as 28 hex digits and 20 zeros (the
+    reference's mode-0 print form, 14 bytes)."""
+    x = (Fraction(hi) + Fraction(lo)) % 1
+    v = int(x * (1 << 112))
+    return format(v, "028x") + "0" * 20
+
+
+def main():
+    big = "--big" in sys.argv
+    path = os.path.join(HERE, "ref_outputs.json")
+    data = json.load(open(path)) if os.path.exists(path) else {}
+    data["source"] = ("reference kernels Bellard.cl / Bellard_div2by1.cl compiled as C++ (oracle/ref_harness), "
+                      "64 work-groups x 256 work-items, launch sequence of KernelFuncs.as")
+    for p in (BIG if big else POSITIONS):
+        e = {}
+        for prec in (0, 1, 2):
+            r = R.run(p, prec)
+            e["d"] = r["d"]
+            e["mode%d" % prec] = dd_hex(*r["dd"]) if prec == 0 else r["hex"]
+            e["mode%d_seconds" % prec] = r["seconds"]
+        data[str(p)] = e
+        json.dump(data, open(path, "w"), indent=1, sort_keys=True)
+        print(p, e, flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -160,3 +160,18 @@ def test_launch_count_counts_kernels(ctx192):
     ctx192.run_prepared()
     ctx192.wait()
     assert ctx192.launch_count - n0 == 2
+
+
+def test_against_reference_kernels(ctx192, ctxdd):
+    """GPU results against the reference's own kernels run on the CPU: the
+    192-bit modes agree for >= 24 hex digits (the spec bar), the
+    106-bit mode for >= 19."""
+    ref = load_golden("ref_outputs.json")
+    for p, e in ref.items():
+        if not p.isdigit():
+            continue
+        h = ctx192.compute(int(p))
+        assert agree(h, e["mode2"]) >= 24, p
+        assert agree(h, e["mode1"]) >= 24, p
+        if int(p) <= 10 ** 7:
+            assert agree(ctxdd.compute(int(p)), e["mode0"]) >= 19, p

@@ -130,3 +130,35 @@ def test_dd_oracle_digits_kept(oracle):
     x = (int(hi * (1 << 100)) << 92) + int(lo * (1 << 192))   # approximate 192-bit image
     exact = oracle.to_hex(oracle.result(d, 0, 4), 4)
     assert agree(format(x % (1 << 192), "048x"), exact) >= 20
+
+
+def test_oracle_against_reference_kernels(oracle):
+    """The reference's own kernels run on the CPU (tests/golden/ref_outputs.json,
+    made by tests/golden/make_ref_golden.py) against the exact oracle."""
+    from oracle.oracle import agreeing_hex_digits as agree
+    ref = load_golden("ref_outputs.json")
+    small = load_golden("oracle_small.json")
+    for p, e in ref.items():
+        if not p.isdigit():
+            continue
+        d, _ = oracle.pos_to_d(int(p))
+        assert e["d"] == d
+        exact = small[p]["hex256"] if p in small else oracle.to_hex(oracle.result(d, 0, 4), 4)
+        # 192-bit modes (dd pairs below 2^32, exact quotients above) keep >= 36 hex digits
+        assert agree(e["mode1"], exact) >= 36, p
+        assert agree(e["mode2"], exact) >= 36, p
+        # the 106-bit mode keeps >= 20
+        assert agree(e["mode0"], exact) >= 20, p
+        assert e["mode0"].endswith("0" * 20)
+
+
+def test_reference_outputs_match_survey_record():
+    """The harness reproduces the reference outputs recorded in the survey."""
+    ref = load_golden("ref_outputs.json")
+    s = load_golden("survey_probe.json")
+    for p, h in s["ref_mode2"].items():
+        if p in ref:
+            assert ref[p]["mode2"] == h
+    for p, h in s["ref_mode0_prefix"].items():
+        if p in ref:
+            assert ref[p]["mode0"].startswith(h)
