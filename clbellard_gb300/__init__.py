@@ -81,6 +81,11 @@ def load(build_if_missing: bool = True):
         "cbl_prepare": ([vp, P64, c_int], c_int),
         "cbl_run_prepared": ([vp], c_int),
         "cbl_kernel_ms": ([vp, ctypes.POINTER(ctypes.c_float)], c_int),
+        "cbl_run_prepared_budget": ([vp, ctypes.c_double, P64, P64], c_int),
+        "cbl_checkpoint_size": ([vp], i64),
+        "cbl_checkpoint_save": ([vp, vp, i64], c_int),
+        "cbl_checkpoint_load": ([vp, vp, i64], c_int),
+        "cbl_set_graph": ([vp, c_int], c_int),
         "cbl_read_results": ([vp, P64], c_int),
         "cbl_prepared_info": ([vp, P64, P64, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
         "cbl_probe_imad": ([vp, c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)], c_int),
@@ -267,6 +272,26 @@ class Context:
 
     def run_prepared(self):
         _check(load().cbl_run_prepared(self._h), "run_prepared")
+
+    def run_prepared_budget(self, budget_ms: float):
+        """Run or continue a pass for about budget_ms; (tiles_done, tiles_total)."""
+        done, total = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(load().cbl_run_prepared_budget(self._h, budget_ms, ctypes.byref(done), ctypes.byref(total)),
+               "run_prepared_budget")
+        return done.value, total.value
+
+    def checkpoint(self) -> bytes:
+        n = _check(load().cbl_checkpoint_size(self._h), "checkpoint_size")
+        buf = ctypes.create_string_buffer(n)
+        _check(load().cbl_checkpoint_save(self._h, buf, n), "checkpoint_save")
+        return buf.raw
+
+    def restore(self, blob: bytes):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        _check(load().cbl_checkpoint_load(self._h, buf, len(blob)), "checkpoint_load")
+
+    def set_graph(self, enable: bool):
+        _check(load().cbl_set_graph(self._h, 1 if enable else 0), "set_graph")
 
     def kernel_ms(self) -> float:
         """Device time (CUDA events) of the term kernel in the last run_prepared."""

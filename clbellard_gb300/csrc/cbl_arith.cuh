@@ -14,9 +14,10 @@
 // (exact division by the odd m), so q_j is the Montgomery multiplier of the
 // step and no division is ever executed. The chain ends at r_0 = 2^(10e) mod m.
 //
-// Four residue kinds:
+// Five residue kinds:
 //   width 1 (m < 2^28): R = 2^32, residues kept lazily in [0, 4m).
-//   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m).
+//   middle width 1 (2^28 <= m < 2^31): R = 2^32, residues in [0, m).
+//   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m), carries kept.
 //   short width 2 (2^32 <= m < 2^40): R = 2^64, residues in [0, 4m).
 //   width 2 (2^28 <= m < 2^50): R = 2^64 by two word steps, residues in [0, 4m).
 // The ladder step is y <- REDC(y^2) << b with b the next exponent bit; in the
@@ -206,6 +207,79 @@ __device__ __forceinline__ uint32_t w1s_pow2(uint64_t E, uint32_t m, uint32_t mp
 {
     W1SState st{w1s_start(m), m, mp};
     walk_bits(E - 32, st);
+    return st.y;
+}
+
+// ------------------------------------------------------ middle width 1 --
+// 2^28 <= m < 2^31: R = 2^32, residues in [0, m). y^2 + u m < 2^64, so the
+// reduction is one multiply-add with y^2 as its addend and no carry handling;
+// REDC < 2m and the doubling < 2m are brought back below m by min(x, x - m).
+__device__ __forceinline__ uint32_t w1m_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
+{
+    const uint64_t t = (uint64_t)y * y;
+    const uint32_t u = (uint32_t)t * mp;
+    const uint32_t z = (uint32_t)(((uint64_t)u * m + t) >> 32);    // < 2m
+    const uint32_t r = min(z, z - m);                               // < m < 2^31
+    const uint32_t x = r << b;                                      // < 2m
+    return min(x, x - m);
+}
+
+struct W1MState {
+    uint32_t y, m, mp;
+    __device__ __forceinline__ void step(uint32_t b) { y = w1m_sqr(y, m, mp, b); }
+};
+
+// 2^(32 + p) mod m in [0, m), 1 <= p <= 7, 2^28 <= m < 2^31: q1 <= 2^11 is off
+// by at most one, so one correction either way suffices.
+__device__ __forceinline__ uint32_t w1m_start(uint32_t m, uint32_t p)
+{
+    const float inv = rcp_approx(__uint2float_rn(m));
+    const float scale = __int_as_float((int)((127u + 32u + p) << 23));
+    const uint32_t q1 = __float2uint_rz(scale * inv);
+    int64_t r = (int64_t)(1ull << (32 + p)) - (int64_t)q1 * (int64_t)m;   // in [-m, 2m)
+    r += (r < 0) ? (int64_t)m : 0;
+    r -= (r >= (int64_t)m) ? (int64_t)m : 0;
+    return (uint32_t)r;
+}
+
+// Start from the leading up-to-three bits of Ep at once (value p), then walk
+// the rest; st.y is set by start(p).
+template <typename State, typename Start>
+__device__ __forceinline__ void walk_bits_p3(uint64_t Ep, State &st, Start start)
+{
+    const uint32_t hi = (uint32_t)(Ep >> 32), lo = (uint32_t)Ep;
+    if (hi != 0) {
+        const int nb = 32 - __clz(hi);
+        const int t = nb < 3 ? nb : 3;
+        start(st, hi >> (nb - t));
+        uint32_t h = (nb - t) > 0 ? hi << (32 - (nb - t)) : 0u;
+        for (int i = t; i < nb; ++i) {
+            st.step(h >> 31);
+            h <<= 1;
+        }
+#pragma unroll
+        for (int i = 31; i >= 0; --i) st.step((lo >> i) & 1u);
+    } else {
+        const int nb = 32 - __clz(lo);
+        const int t = nb < 3 ? nb : 3;
+        start(st, lo >> (nb - t));
+        uint32_t l = (nb - t) > 0 ? lo << (32 - (nb - t)) : 0u;
+        for (int i = t; i < nb; ++i) {
+            st.step(l >> 31);
+            l <<= 1;
+        }
+    }
+}
+
+struct W1MStart {
+    __device__ __forceinline__ void operator()(W1MState &st, uint32_t p) const { st.y = w1m_start(st.m, p); }
+};
+
+// r6 = 2^E mod m in [0, m) for E >= 33, 2^28 <= m < 2^31.
+__device__ __forceinline__ uint32_t w1m_pow2(uint64_t E, uint32_t m, uint32_t mp)
+{
+    W1MState st{0, m, mp};
+    walk_bits_p3(E - 32, st, W1MStart{});
     return st.y;
 }
 

@@ -59,6 +59,10 @@ struct cbl_ctx {
     uint64_t prep_terms = 0;
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;   // around the term kernel of the last prepared run
     bool ev_valid = false;
+    cudaGraphExec_t graph = nullptr;                 // captured prepared pass
+    bool use_graph = true;
+    int partial = 0;                                 // a budgeted run is in progress
+    uint64_t seg_hash = 0;                           // identity of the prepared tile table
     // double-double buffers
     double2 *d_bigsum = nullptr;
     double2 *d_ddpartial = nullptr;
@@ -76,6 +80,12 @@ struct cbl_ctx {
 namespace {
 
 bool is192(const cbl_ctx *c) { return c->precision != 0; }
+
+void drop_graph(cbl_ctx *c)
+{
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+}
 
 int ensure_segs(cbl_ctx *c, int n)
 {
@@ -135,7 +145,7 @@ bool series_ok(uint64_t den0, uint64_t den1)
 }
 
 // Append the segments covering k in [k0, k1) of one series, split at d (main
-// vs tail) and at the residue-kind boundaries m = 2^28, 2^32 and 2^40. k = 0 with
+// vs tail) and at the residue-kind boundaries m = 2^28, 2^31, 2^32 and 2^40. k = 0 with
 // den1 = 1 (m = 1) contributes exactly 0 and is left out.
 int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, int sign, uint32_t slot,
                  uint64_t k0, uint64_t k1)
@@ -144,10 +154,11 @@ int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, 
     if (k1 <= k0) return CBL_OK;
     if ((u128)den0 * (k1 - 1) + den1 >= (u128)kW2Max) return CBL_E_POSITION;
     const uint64_t kw1 = (kW1Max - den1 + den0 - 1) / den0;    // first k with m >= 2^28
+    const uint64_t kw1m = (kW1MMax - den1 + den0 - 1) / den0;  // first k with m >= 2^31
     const uint64_t kw1s = (kW1SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^32
     const uint64_t kw2s = (kW2SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^40
     std::vector<uint64_t> pts = {k0, k1};
-    for (uint64_t c : {d, kw1, kw1s, kw2s}) pts.push_back(std::min(std::max(c, k0), k1));
+    for (uint64_t c : {d, kw1, kw1m, kw1s, kw2s}) pts.push_back(std::min(std::max(c, k0), k1));
     std::sort(pts.begin(), pts.end());
     for (size_t i = 0; i + 1 < pts.size(); ++i) {
         const uint64_t a = pts[i], b = pts[i + 1];
@@ -159,17 +170,23 @@ int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, 
         s.den0 = den0;
         s.den1 = den1;
         s.slot = slot;
-        s.flags = seg_flags(sign, a >= kw2s ? 2 : (a >= kw1s ? 4 : (a >= kw1 ? 3 : 1)));
+        s.flags = seg_flags(sign, a >= kw2s ? 2 : (a >= kw1s ? 4 : (a >= kw1m ? 3 : (a >= kw1 ? 5 : 1))));
         v.push_back(s);
     }
     return CBL_OK;
 }
 
-// Cost rank of a residue kind: width 2 > short width 2 > strict width 1 > width 1.
+// Cost rank of a residue kind: width 2 > short width 2 > strict width 1 >
+// middle width 1 > width 1.
 int kind_rank(uint32_t flags)
 {
-    const uint32_t k = (flags >> 4) & 15u;
-    return k == 2 ? 3 : (k == 4 ? 2 : (k == 3 ? 1 : 0));
+    switch ((flags >> 4) & 15u) {
+    case 2: return 4;
+    case 4: return 3;
+    case 3: return 2;
+    case 5: return 1;
+    default: return 0;
+    }
 }
 
 // Costlier tiles first (width 2, then large d), tails last; then tile prefixes.
@@ -405,6 +422,7 @@ int cbl_destroy(cbl_ctx *c)
     cudaFree(c->d_ddpartial);
     cudaFree(c->d_ddans);
     cudaFreeHost(c->h_small);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->ev_k0) cudaEventDestroy(c->ev_k0);
     if (c->ev_k1) cudaEventDestroy(c->ev_k1);
     if (c->st) cudaStreamDestroy(c->st);
@@ -426,8 +444,18 @@ int cbl_device_name(const cbl_ctx *c, char *buf, int len)
 int cbl_set_tuning(cbl_ctx *c, int tile_terms, int ctas_per_sm)
 {
     if (!c || tile_terms < 32 || tile_terms % 32 != 0 || ctas_per_sm < 0) return CBL_E_ARG;
+    if (c->partial) return CBL_E_ARG;                 // a budgeted run depends on the tile numbering
     c->tile_k = tile_terms;
     c->ctas_per_sm = ctas_per_sm;
+    drop_graph(c);
+    return CBL_OK;
+}
+
+int cbl_set_graph(cbl_ctx *c, int enable)
+{
+    if (!c) return CBL_E_ARG;
+    c->use_graph = enable != 0;
+    drop_graph(c);
     return CBL_OK;
 }
 
@@ -602,6 +630,13 @@ int cbl_wait(cbl_ctx *c, int timeout_ms)
     }
 }
 
+static uint64_t fnv1a(const void *p, size_t n, uint64_t h = 1469598103934665603ull)
+{
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+}
+
 // Build and upload the segments of all 7 series of n positions (d[i],
 // shift[i]); slots i*7+f. Nothing is launched.
 static int prepare_positions(cbl_ctx *c, const uint64_t *d, const int *shift, int n)
@@ -627,27 +662,62 @@ static int prepare_positions(cbl_ctx *c, const uint64_t *d, const int *shift, in
     std::memcpy(c->h_out3, shift, sizeof(int) * n);          // pinned staging for the shifts
     CK(cudaMemcpyAsync(c->d_shift, c->h_out3, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
+    drop_graph(c);
     c->prep_npos = n;
     c->prep_nseg = (int)v.size();
     c->prep_ntiles = ntiles;
     c->prep_terms = terms;
+    c->partial = 0;
+    c->seg_hash = fnv1a(shift, sizeof(int) * n, fnv1a(v.data(), sizeof(Seg) * v.size()));
     return CBL_OK;
 }
 
-// Enqueue the prepared run: zero slots and tile counter, the persistent term
-// kernel, the combine kernel. Results land in d_out3.
-static int launch_prepared(cbl_ctx *c)
+// Enqueue the prepared pass: zero slots and tile counter, the persistent term
+// kernel between two events, the combine kernel. The first pass after a
+// prepare is captured into a CUDA graph and every later pass replays it.
+static int enqueue_prepared(cbl_ctx *c, bool capturing)
 {
+    // inside a capture the events must be external records so that the graph
+    // records them when it is replayed; outside a capture that flag is refused
+    const unsigned int evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     const int n = c->prep_npos;
-    if (n <= 0) return CBL_E_ARG;
     CK(cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6 * 7 * n, c->st));
     CK(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), c->st));
-    CK(cudaEventRecord(c->ev_k0, c->st));
+    CK(cudaEventRecordWithFlags(c->ev_k0, c->st, evf));
     CK(launch_terms192(c->d_segs, c->prep_nseg, c->prep_ntiles, (uint32_t)c->tile_k, c->d_counter, c->d_slots,
                        grid_192(c), 256, c->st));
-    CK(cudaEventRecord(c->ev_k1, c->st));
-    c->ev_valid = true;
+    CK(cudaEventRecordWithFlags(c->ev_k1, c->st, evf));
     CK(launch_combine(c->d_slots, n, c->d_shift, c->d_out3, nullptr, c->st));
+    return CBL_OK;
+}
+
+static int launch_prepared(cbl_ctx *c)
+{
+    if (c->prep_npos <= 0) return CBL_E_ARG;
+    c->partial = 0;
+    if (c->use_graph) {
+        if (!c->graph) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+            const int rc = enqueue_prepared(c, true);
+            const cudaError_t e = cudaStreamEndCapture(c->st, &g);
+            if (rc || e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return rc ? rc : CBL_E_CUDA;
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&c->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                c->graph = nullptr;
+                return CBL_E_CUDA;
+            }
+        }
+        CK(cudaGraphLaunch(c->graph, c->st));
+    } else {
+        const int rc = enqueue_prepared(c, false);
+        if (rc) return rc;
+    }
+    c->ev_valid = true;
     c->launches += 2;
     return CBL_OK;
 }
@@ -894,6 +964,83 @@ int cbl_prepared_info(const cbl_ctx *c, uint64_t *terms, uint64_t *tiles, int *s
     if (tiles) *tiles = c->prep_ntiles;
     if (segments) *segments = c->prep_nseg;
     if (grid) *grid = grid_192(const_cast<cbl_ctx *>(c));
+    return CBL_OK;
+}
+
+int cbl_run_prepared_budget(cbl_ctx *c, double budget_ms, uint64_t *tiles_done, uint64_t *tiles_total)
+{
+    if (!c || budget_ms <= 0 || c->prep_npos <= 0) return CBL_E_ARG;
+    cudaSetDevice(c->device);
+    const int n = c->prep_npos;
+    if (!c->partial) {                                    // a fresh pass
+        CK(cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6 * 7 * n, c->st));
+        CK(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), c->st));
+        c->partial = 1;
+    }
+    const uint64_t budget_ns = (uint64_t)(budget_ms * 1e6) + 1;
+    CK(launch_terms192(c->d_segs, c->prep_nseg, c->prep_ntiles, (uint32_t)c->tile_k, c->d_counter, c->d_slots,
+                       grid_192(c), 256, c->st, budget_ns));
+    c->launches++;
+    CK(cudaMemcpyAsync(c->h_small, c->d_counter, sizeof(uint64_t), cudaMemcpyDeviceToHost, c->st));
+    int rc = sync(c);
+    if (rc) return rc;
+    const uint64_t done = std::min<uint64_t>(c->h_small[0], c->prep_ntiles);
+    if (done >= c->prep_ntiles) {
+        CK(launch_combine(c->d_slots, n, c->d_shift, c->d_out3, nullptr, c->st));
+        c->launches++;
+        c->partial = 0;
+    }
+    if (tiles_done) *tiles_done = done;
+    if (tiles_total) *tiles_total = c->prep_ntiles;
+    return CBL_OK;
+}
+
+// Checkpoint of a budgeted run: header, tiles done, the slots' digit sums.
+struct CkptHeader {
+    uint64_t magic, hash, npos, ntiles, done;
+};
+static const uint64_t kCkptMagic = 0x31544b50434c4243ull;   // "CBLCPKT1"
+
+int64_t cbl_checkpoint_size(const cbl_ctx *c)
+{
+    if (!c || c->prep_npos <= 0) return CBL_E_ARG;
+    return (int64_t)(sizeof(CkptHeader) + sizeof(unsigned long long) * 6 * 7 * c->prep_npos);
+}
+
+int cbl_checkpoint_save(cbl_ctx *c, void *buf, int64_t size)
+{
+    if (!c || !buf || c->prep_npos <= 0 || size < cbl_checkpoint_size(c)) return CBL_E_ARG;
+    cudaSetDevice(c->device);
+    int rc = sync(c);
+    if (rc) return rc;
+    CkptHeader h{kCkptMagic, c->seg_hash, (uint64_t)c->prep_npos, c->prep_ntiles, 0};
+    if (c->partial) {
+        CK(cudaMemcpy(&h.done, c->d_counter, sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        h.done = std::min<uint64_t>(h.done, c->prep_ntiles);
+    }
+    std::memcpy(buf, &h, sizeof h);
+    if (c->partial)
+        CK(cudaMemcpy(static_cast<char *>(buf) + sizeof h, c->d_slots, sizeof(unsigned long long) * 6 * 7 * c->prep_npos,
+                      cudaMemcpyDeviceToHost));
+    else
+        std::memset(static_cast<char *>(buf) + sizeof h, 0, sizeof(unsigned long long) * 6 * 7 * c->prep_npos);
+    return CBL_OK;
+}
+
+int cbl_checkpoint_load(cbl_ctx *c, const void *buf, int64_t size)
+{
+    if (!c || !buf || c->prep_npos <= 0 || size < cbl_checkpoint_size(c)) return CBL_E_ARG;
+    CkptHeader h;
+    std::memcpy(&h, buf, sizeof h);
+    if (h.magic != kCkptMagic) return CBL_E_FORMAT;
+    if (h.hash != c->seg_hash || h.npos != (uint64_t)c->prep_npos || h.ntiles != c->prep_ntiles || h.done > h.ntiles)
+        return CBL_E_FORMAT;                               // not a checkpoint of this prepared run
+    cudaSetDevice(c->device);
+    CK(cudaMemcpy(c->d_slots, static_cast<const char *>(buf) + sizeof h,
+                  sizeof(unsigned long long) * 6 * 7 * c->prep_npos, cudaMemcpyHostToDevice));
+    const unsigned long long done = h.done;
+    CK(cudaMemcpy(c->d_counter, &done, sizeof done, cudaMemcpyHostToDevice));
+    c->partial = 1;
     return CBL_OK;
 }
 

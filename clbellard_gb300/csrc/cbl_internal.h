@@ -15,7 +15,8 @@ constexpr uint32_t kDen1[7] = {1, 3, 1, 3, 5, 7, 9};
 
 // Residue-width limits of the term kernels (m odd, m >= 3).
 constexpr uint64_t kW1Max = 1ull << 28;   // width 1 (one 32-bit word) for m < 2^28
-constexpr uint64_t kW1SMax = 1ull << 32;  // strict width 1 for 2^28 <= m < 2^32
+constexpr uint64_t kW1MMax = 1ull << 31;  // middle width 1 for 2^28 <= m < 2^31
+constexpr uint64_t kW1SMax = 1ull << 32;  // strict width 1 for 2^31 <= m < 2^32
 constexpr uint64_t kW2SMax = 1ull << 40;  // short width 2 for 2^32 <= m < 2^40
 constexpr uint64_t kW2Max = 1ull << 50;   // width 2 (two words) for m < 2^50
 
@@ -31,7 +32,7 @@ struct Seg {
     uint64_t tile0;
     uint32_t den0, den1;
     uint32_t slot;         // accumulator slot (6 x u64 digit sums)
-    uint32_t flags;        // bit 0: series sign (1 = minus), bits 4-7: residue kind 1|2|3|4
+    uint32_t flags;        // bit 0: series sign (1 = minus), bits 4-7: residue kind 1..5
 };
 static_assert(sizeof(Seg) == 48, "Seg layout");
 
@@ -39,9 +40,11 @@ constexpr uint32_t kFlagSign = 1u;
 inline uint32_t seg_flags(int sign, int width) { return (uint32_t)(sign & 1) | ((uint32_t)width << 4); }
 
 // Launch wrappers (cbl_kernels.cu).
+// budget_ns = 0: run to the end; else warps stop taking tiles after budget_ns
+// and the finished tiles are [0, *counter).
 cudaError_t launch_terms192(const Seg *segs, int nseg, uint64_t ntiles, uint32_t tile_k,
-                            unsigned long long *counter, unsigned long long *slots, int grid,
-                            int block, cudaStream_t st);
+                            unsigned long long *counter, unsigned long long *slots, int grid, int block,
+                            cudaStream_t st, uint64_t budget_ns = 0);
 // slots (nslot x 6 digit sums) of position i, series f = slots[(slot_base[i] + f) * 6 ..]:
 // out3[3i..3i+2] (word 0 most significant) = sum_f (S_f << (numer_log2[f] + shift[i])).
 // If partial7 != nullptr it also receives the 7 weighted partials per position.

@@ -48,8 +48,9 @@ __device__ __forceinline__ void shr192(uint32_t q[6], int s)
 
 // One term's six quotient digits: k < d gives frac(2^(10(d-k))/m), k >= d the
 // tail value 2^(-10(k-d))/m (digits of 1/m shifted right by 10(k-d)).
-// KIND: 1 = width 1 (m < 2^28), 3 = strict width 1 (2^28 <= m < 2^32),
-// 4 = short width 2 (2^32 <= m < 2^40), 2 = width 2 (2^28 <= m < 2^50).
+// KIND: 1 = width 1 (m < 2^28), 5 = middle width 1 (2^28 <= m < 2^31),
+// 3 = strict width 1 (2^28 <= m < 2^32), 4 = short width 2 (2^32 <= m < 2^40),
+// 2 = width 2 (2^28 <= m < 2^50).
 template <int KIND, bool TAIL>
 __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, uint32_t q[6])
 {
@@ -57,6 +58,9 @@ __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, 
     const uint64_t E = TAIL ? 192ull : 10ull * (d - k) + 192ull;
     if (KIND == 1) {
         const uint32_t r6 = w1_pow2(E, (uint32_t)m, mp);
+        w1_digits(r6, (uint32_t)m, mp, q);
+    } else if (KIND == 5) {
+        const uint32_t r6 = w1m_pow2(E, (uint32_t)m, mp);
         w1_digits(r6, (uint32_t)m, mp, q);
     } else if (KIND == 3) {
         const uint32_t r6 = w1s_pow2(E, (uint32_t)m, mp);
@@ -107,16 +111,31 @@ __device__ __forceinline__ void warp_flush(const Acc192 &acc, int lane, unsigned
     }
 }
 
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // ------------------------------------------------------- terms192 kernel --
+// With budget_ns != 0 a warp takes no new tile once budget_ns have passed
+// since it started. The deadline is checked before the tile counter is
+// incremented, so every tile taken is finished and the finished tiles are
+// exactly [0, counter): a later launch continues from there.
 __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restrict__ segs, int nseg,
                                                              uint64_t ntiles, uint32_t tile_k,
                                                              unsigned long long *counter,
-                                                             unsigned long long *slots)
+                                                             unsigned long long *slots, uint64_t budget_ns)
 {
     const int lane = threadIdx.x & 31;
+    const uint64_t t_start = budget_ns ? global_ns() : 0;
     for (;;) {
         unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(counter, 1ull);
+        if (lane == 0) {
+            if (budget_ns && global_ns() - t_start > budget_ns) t = ~0ull;
+            else t = atomicAdd(counter, 1ull);
+        }
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= ntiles) break;
         int lo = 0, hi = nseg - 1;
@@ -134,11 +153,13 @@ __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restri
         uint32_t cnt = 0;
         if (tail) {
             if (width == 1) run_tile<1, true>(s, kb, ke, lane, acc, cnt);
+            else if (width == 5) run_tile<5, true>(s, kb, ke, lane, acc, cnt);
             else if (width == 3) run_tile<3, true>(s, kb, ke, lane, acc, cnt);
             else if (width == 4) run_tile<4, true>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, true>(s, kb, ke, lane, acc, cnt);
         } else {
             if (width == 1) run_tile<1, false>(s, kb, ke, lane, acc, cnt);
+            else if (width == 5) run_tile<5, false>(s, kb, ke, lane, acc, cnt);
             else if (width == 3) run_tile<3, false>(s, kb, ke, lane, acc, cnt);
             else if (width == 4) run_tile<4, false>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, false>(s, kb, ke, lane, acc, cnt);
@@ -151,10 +172,10 @@ __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restri
 
 cudaError_t launch_terms192(const Seg *segs, int nseg, uint64_t ntiles, uint32_t tile_k,
                             unsigned long long *counter, unsigned long long *slots, int grid, int block,
-                            cudaStream_t st)
+                            cudaStream_t st, uint64_t budget_ns)
 {
     (void)block;
-    terms192_kernel<<<grid, kBlock192, 0, st>>>(segs, nseg, ntiles, tile_k, counter, slots);
+    terms192_kernel<<<grid, kBlock192, 0, st>>>(segs, nseg, ntiles, tile_k, counter, slots, budget_ns);
     return cudaGetLastError();
 }
 
@@ -281,11 +302,13 @@ __global__ void terms_each_kernel(uint64_t d, uint32_t den0, uint32_t den1, int 
     if (m != 1) {
         if (k < d) {
             if (m < kW1Max) term_digits<1, false>(d, k, m, q);
+            else if (m < kW1MMax) term_digits<5, false>(d, k, m, q);
             else if (m < kW1SMax) term_digits<3, false>(d, k, m, q);
             else if (m < kW2SMax) term_digits<4, false>(d, k, m, q);
             else term_digits<2, false>(d, k, m, q);
         } else {
             if (m < kW1Max) term_digits<1, true>(d, k, m, q);
+            else if (m < kW1MMax) term_digits<5, true>(d, k, m, q);
             else if (m < kW1SMax) term_digits<3, true>(d, k, m, q);
             else if (m < kW2SMax) term_digits<4, true>(d, k, m, q);
             else term_digits<2, true>(d, k, m, q);
@@ -374,6 +397,7 @@ __global__ void __launch_bounds__(kBlockDD) dd_terms_kernel(double2 *bigsum, uin
         uint32_t q[6];
         uint64_t r;
         if (m < kW1Max) r = w1_digits(w1_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
+        else if (m < kW1MMax) r = w1_digits(w1m_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
         else if (m < kW1SMax) r = w1_digits(w1s_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
         else if (m < kW2SMax) r = w2_digits(w2s_pow2(E, m, mp), m, mp, q);
         else r = w2_digits(w2_pow2(E, m, mp), m, mp, q);

@@ -137,6 +137,23 @@ int cbl_prepare(cbl_ctx *ctx, const uint64_t *pos, int n);
 int cbl_run_prepared(cbl_ctx *ctx);
 /* Copy the prepared positions' results (3 words each, most significant first). */
 int cbl_read_results(cbl_ctx *ctx, uint64_t *out3n);
+/* Bounded-time pass (the reference's "GPU 99% load" launch splitting,
+ * Bellard_192.hsp:74, KernelFuncs.as:36-51): starts a pass over the prepared
+ * positions, or continues the one in progress, for about budget_ms of device
+ * time, waits, and reports the warp tiles finished so far. When
+ * tiles_done == tiles_total the results are ready for cbl_read_results.
+ * Resumed passes give the same bits as an uninterrupted one. */
+int cbl_run_prepared_budget(cbl_ctx *ctx, double budget_ms, uint64_t *tiles_done, uint64_t *tiles_total);
+/* Checkpoint of a pass in progress (on-device 192-bit partial sums and the
+ * tiles finished): size, save to a host buffer, load into a context that has
+ * prepared the same positions (CBL_E_FORMAT otherwise), then continue with
+ * cbl_run_prepared_budget. */
+int64_t cbl_checkpoint_size(const cbl_ctx *ctx);
+int cbl_checkpoint_save(cbl_ctx *ctx, void *buf, int64_t size);
+int cbl_checkpoint_load(cbl_ctx *ctx, const void *buf, int64_t size);
+/* cbl_run_prepared replays a CUDA graph captured on its first call after
+ * cbl_prepare (enable = 1, the default); 0 launches the kernels directly. */
+int cbl_set_graph(cbl_ctx *ctx, int enable);
 /* Device time of the term kernel in the last cbl_run_prepared (CUDA events on
  * the context's stream around that launch); waits for it to finish. */
 int cbl_kernel_ms(cbl_ctx *ctx, float *ms);

@@ -1,0 +1,55 @@
+"""Bounded-time passes, checkpoints and graph replay: interrupted and
+resumed passes give the same bits as uninterrupted ones."""
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def want(p):
+    return int(load_golden("oracle_big.json")[str(p)]["hex192"], 16)
+
+
+def test_budgeted_pass_resumes_bit_exactly(ctx192):
+    ctx192.prepare([10 ** 9])
+    steps, done, total = 0, 0, 1
+    while done < total:
+        done, total = ctx192.run_prepared_budget(4.0)
+        steps += 1
+        assert steps < 10000
+    assert steps > 3                      # the budget really split the pass
+    assert ctx192.read_results()[0] == want(10 ** 9)
+
+
+def test_checkpoint_restore_in_new_context(cbl):
+    with cbl.Context(0, 1) as a:
+        a.prepare([10 ** 8])
+        done, total = a.run_prepared_budget(1.0)
+        assert 0 < done < total
+        blob = a.checkpoint()
+    with cbl.Context(0, 1) as b:
+        b.prepare([10 ** 8])
+        b.restore(blob)
+        while done < total:
+            done, total = b.run_prepared_budget(50.0)
+        assert b.read_results()[0] == want(10 ** 8)
+        b.prepare([10 ** 8 + 10])          # a different tile table refuses the checkpoint
+        with pytest.raises(cbl.CblError) as e:
+            b.restore(blob)
+        assert e.value.code == -10
+
+
+def test_graph_replay_equals_direct_launch(ctx192):
+    ctx192.prepare([123455, 10 ** 6])
+    ctx192.set_graph(False)
+    ctx192.run_prepared()
+    ctx192.wait()
+    direct = ctx192.read_results()
+    ctx192.set_graph(True)
+    for _ in range(3):
+        ctx192.run_prepared()
+    ctx192.wait()
+    assert ctx192.kernel_ms() > 0.0                  # events inside the replayed graph
+    assert ctx192.read_results() == direct
+    assert "%048x" % direct[1] == load_golden("oracle_small.json")["1000000"]["hex192"]

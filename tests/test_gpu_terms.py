@@ -34,6 +34,15 @@ def test_terms_width_boundary(ctx192, oracle, f):
 
 
 @pytest.mark.parametrize("f", range(7))
+def test_terms_31bit_boundary(ctx192, oracle, f):
+    """k around the first modulus >= 2^31 (middle -> strict width 1)."""
+    den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
+    k31 = ((1 << 31) - den1 + den0 - 1) // den0
+    for d in (3999999999, k31 + 3, k31 + 40):
+        check_terms(ctx192, oracle, d, f, [k for k in range(k31 - 40, k31 + 40) if k < d + 20])
+
+
+@pytest.mark.parametrize("f", range(7))
 def test_terms_32bit_boundary(ctx192, oracle, f):
     """k around the first modulus >= 2^32 (strict width 1 -> width 2)."""
     den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
