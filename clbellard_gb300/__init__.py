@@ -86,6 +86,8 @@ def load(build_if_missing: bool = True):
         "cbl_checkpoint_save": ([vp, vp, i64], c_int),
         "cbl_checkpoint_load": ([vp, vp, i64], c_int),
         "cbl_set_graph": ([vp, c_int], c_int),
+        "cbl_autotune": ([vp, P64, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                          ctypes.POINTER(ctypes.c_double)], c_int),
         "cbl_read_results": ([vp, P64], c_int),
         "cbl_prepared_info": ([vp, P64, P64, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
         "cbl_probe_imad": ([vp, c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)], c_int),
@@ -289,6 +291,16 @@ class Context:
     def restore(self, blob: bytes):
         buf = ctypes.create_string_buffer(blob, len(blob))
         _check(load().cbl_checkpoint_load(self._h, buf, len(blob)), "checkpoint_load")
+
+    def autotune(self, positions, force: bool = False):
+        """Pick tile size and CTAs/SM for these positions (cached); (tile, ctas, ms)."""
+        n = len(positions)
+        pos = (ctypes.c_uint64 * n)(*positions)
+        t, c, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(load().cbl_autotune(self._h, pos, n, 1 if force else 0, ctypes.byref(t), ctypes.byref(c),
+                                   ctypes.byref(ms)), "autotune")
+        self._prepared = n
+        return t.value, c.value, ms.value
 
     def set_graph(self, enable: bool):
         _check(load().cbl_set_graph(self._h, 1 if enable else 0), "set_graph")

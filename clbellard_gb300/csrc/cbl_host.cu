@@ -63,6 +63,8 @@ struct cbl_ctx {
     bool use_graph = true;
     int partial = 0;                                 // a budgeted run is in progress
     uint64_t seg_hash = 0;                           // identity of the prepared tile table
+    std::vector<Seg> prep_segs;                      // host copy of the prepared segments
+    std::vector<int> prep_shift;
     // double-double buffers
     double2 *d_bigsum = nullptr;
     double2 *d_ddpartial = nullptr;
@@ -70,6 +72,10 @@ struct cbl_ctx {
     // scratch host
     uint64_t *h_small = nullptr;              // pinned, 8 words
 };
+
+extern "C" {
+static int upload_prepared(cbl_ctx *c);
+}
 
 #define CK(x)                                     \
     do {                                          \
@@ -445,9 +451,14 @@ int cbl_set_tuning(cbl_ctx *c, int tile_terms, int ctas_per_sm)
 {
     if (!c || tile_terms < 32 || tile_terms % 32 != 0 || ctas_per_sm < 0) return CBL_E_ARG;
     if (c->partial) return CBL_E_ARG;                 // a budgeted run depends on the tile numbering
+    const bool renumber = tile_terms != c->tile_k && c->prep_npos > 0;
     c->tile_k = tile_terms;
     c->ctas_per_sm = ctas_per_sm;
     drop_graph(c);
+    if (renumber) {
+        cudaSetDevice(c->device);
+        return upload_prepared(c);
+    }
     return CBL_OK;
 }
 
@@ -637,6 +648,29 @@ static uint64_t fnv1a(const void *p, size_t n, uint64_t h = 1469598103934665603u
     return h;
 }
 
+// Number the prepared segments' tiles for the current tile size and upload
+// them with the per-position shifts (again after a tile-size change).
+static int upload_prepared(cbl_ctx *c)
+{
+    std::vector<Seg> &v = c->prep_segs;
+    const int n = c->prep_npos;
+    const uint64_t ntiles = order_and_number(v, (uint32_t)c->tile_k);
+    int rc = ensure_segs(c, (int)v.size());
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->st));
+    std::memcpy(c->h_segs, v.data(), sizeof(Seg) * v.size());
+    CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(Seg) * v.size(), cudaMemcpyHostToDevice, c->st));
+    std::memcpy(c->h_out3, c->prep_shift.data(), sizeof(int) * n);      // pinned staging for the shifts
+    CK(cudaMemcpyAsync(c->d_shift, c->h_out3, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    drop_graph(c);
+    c->prep_nseg = (int)v.size();
+    c->prep_ntiles = ntiles;
+    c->partial = 0;
+    c->seg_hash = fnv1a(c->prep_shift.data(), sizeof(int) * n, fnv1a(v.data(), sizeof(Seg) * v.size()));
+    return CBL_OK;
+}
+
 // Build and upload the segments of all 7 series of n positions (d[i],
 // shift[i]); slots i*7+f. Nothing is launched.
 static int prepare_positions(cbl_ctx *c, const uint64_t *d, const int *shift, int n)
@@ -653,23 +687,11 @@ static int prepare_positions(cbl_ctx *c, const uint64_t *d, const int *shift, in
             rc = add_segments(v, d[i], kDen0[f], kDen1[f], kSign[f], (uint32_t)(i * 7 + f), 0, d[i] + kTail192);
     }
     if (rc) return rc;
-    const uint64_t ntiles = order_and_number(v, (uint32_t)c->tile_k);
-    rc = ensure_segs(c, (int)v.size());
-    if (rc) return rc;
-    CK(cudaStreamSynchronize(c->st));
-    std::memcpy(c->h_segs, v.data(), sizeof(Seg) * v.size());
-    CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(Seg) * v.size(), cudaMemcpyHostToDevice, c->st));
-    std::memcpy(c->h_out3, shift, sizeof(int) * n);          // pinned staging for the shifts
-    CK(cudaMemcpyAsync(c->d_shift, c->h_out3, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    drop_graph(c);
+    c->prep_segs.swap(v);
+    c->prep_shift.assign(shift, shift + n);
     c->prep_npos = n;
-    c->prep_nseg = (int)v.size();
-    c->prep_ntiles = ntiles;
     c->prep_terms = terms;
-    c->partial = 0;
-    c->seg_hash = fnv1a(shift, sizeof(int) * n, fnv1a(v.data(), sizeof(Seg) * v.size()));
-    return CBL_OK;
+    return upload_prepared(c);
 }
 
 // Enqueue the prepared pass: zero slots and tile counter, the persistent term
@@ -964,6 +986,90 @@ int cbl_prepared_info(const cbl_ctx *c, uint64_t *terms, uint64_t *tiles, int *s
     if (tiles) *tiles = c->prep_ntiles;
     if (segments) *segments = c->prep_nseg;
     if (grid) *grid = grid_192(const_cast<cbl_ctx *>(c));
+    return CBL_OK;
+}
+
+// ---- autotuning: tile size x persistent CTAs per SM, timed on the caller's
+// positions, cached per (device name, SM count, positions) in a text file.
+static std::string tune_cache_path()
+{
+    if (const char *p = std::getenv("CBL_TUNE_CACHE")) return p;
+    const char *home = std::getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/clbellard_tune.txt";
+}
+
+static bool tune_cache_lookup(const std::string &key, int *tile, int *ctas)
+{
+    FILE *f = std::fopen(tune_cache_path().c_str(), "r");
+    if (!f) return false;
+    char line[512];
+    bool found = false;
+    while (std::fgets(line, sizeof line, f)) {
+        char k[400];
+        int t, c;
+        if (std::sscanf(line, "%399s %d %d", k, &t, &c) == 3 && key == k) {
+            *tile = t;
+            *ctas = c;
+            found = true;                                    // the last entry wins
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+static void tune_cache_store(const std::string &key, int tile, int ctas)
+{
+    const std::string p = tune_cache_path();
+    const size_t slash = p.rfind('/');
+    if (slash != std::string::npos) mkdir_p(p.substr(0, slash));
+    if (FILE *f = std::fopen(p.c_str(), "a")) {
+        std::fprintf(f, "%s %d %d\n", key.c_str(), tile, ctas);
+        std::fclose(f);
+    }
+}
+
+int cbl_autotune(cbl_ctx *c, const uint64_t *pos, int n, int force, int *best_tile, int *best_ctas, double *best_ms)
+{
+    if (!c || !pos || n <= 0) return CBL_E_ARG;
+    if (!is192(c)) return CBL_E_PRECISION;
+    cudaSetDevice(c->device);
+    char key[400];
+    std::snprintf(key, sizeof key, "%s|sm%d|n%d|h%016llx", c->devname, c->sm_count, n,
+                  (unsigned long long)fnv1a(pos, sizeof(uint64_t) * n));
+    for (char *q = key; *q; ++q)
+        if (*q == ' ') *q = '_';
+    int tile = 0, ctas = 0;
+    double ms_best = -1.0;
+    if (!force && tune_cache_lookup(key, &tile, &ctas)) {
+        int rc = cbl_set_tuning(c, tile, ctas);
+        if (rc) return rc;
+    } else {
+        const int occ = terms192_max_ctas_per_sm(256);
+        const int tiles[] = {512, 1024, 2048, 4096, 8192};
+        ms_best = 1e300;
+        for (int t : tiles) {
+            for (int cc = occ; cc >= 1 && cc >= occ - 2; --cc) {
+                int rc = cbl_set_tuning(c, t, cc);
+                if (!rc) rc = cbl_prepare(c, pos, n);
+                if (!rc) rc = cbl_run_prepared(c);                 // warm-up and graph capture
+                if (!rc) rc = cbl_run_prepared(c);
+                float ms = 0;
+                if (!rc) rc = cbl_kernel_ms(c, &ms);
+                if (rc) return rc;
+                if (ms < ms_best) {
+                    ms_best = ms;
+                    tile = t;
+                    ctas = cc;
+                }
+            }
+        }
+        int rc = cbl_set_tuning(c, tile, ctas);
+        if (rc) return rc;
+        tune_cache_store(key, tile, ctas);
+    }
+    if (best_tile) *best_tile = tile;
+    if (best_ctas) *best_ctas = ctas;
+    if (best_ms) *best_ms = ms_best;
     return CBL_OK;
 }
 

@@ -169,6 +169,14 @@ int cbl_probe_imad(cbl_ctx *ctx, int iters, double *ops_per_s, double *ms);
 int cbl_terms(cbl_ctx *ctx, uint64_t d, int f, const uint64_t *k, int n, uint64_t *out3n);
 /* Kernel launches issued on this context since creation (counts every kernel). */
 int64_t cbl_launch_count(const cbl_ctx *ctx);
+/* Autotuner: times one pass over pos[0..n) for each warp-tile size
+ * (512..8192 terms) and persistent CTAs per SM (the occupancy limit and two
+ * below it), keeps the fastest (cbl_set_tuning) and appends it to a cache
+ * file ($CBL_TUNE_CACHE, default ~/.cache/clbellard_tune.txt) keyed by device,
+ * SM count and positions; a cached entry is reused unless force != 0
+ * (*best_ms is then -1). Leaves the context prepared for pos. */
+int cbl_autotune(cbl_ctx *ctx, const uint64_t *pos, int n, int force, int *best_tile, int *best_ctas,
+                 double *best_ms);
 /* Tuning: terms per warp tile (multiple of 32) and persistent CTAs per SM (0 = auto). */
 int cbl_set_tuning(cbl_ctx *ctx, int tile_terms, int ctas_per_sm);
 const char *cbl_strerror(int code);

@@ -175,3 +175,18 @@ def test_against_reference_kernels(ctx192, ctxdd):
         assert agree(h, e["mode1"]) >= 24, p
         if int(p) <= 10 ** 7:
             assert agree(ctxdd.compute(int(p)), e["mode0"]) >= 19, p
+
+
+def test_autotune_keeps_bits(cbl, tmp_path, monkeypatch):
+    monkeypatch.setenv("CBL_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    pos = [1000, 123455, 10 ** 6]
+    with cbl.Context(0, 1) as ctx:
+        want = ctx.batch(pos)
+        tile, ctas, ms = ctx.autotune(pos, force=True)
+        assert tile in (512, 1024, 2048, 4096, 8192) and ctas >= 1 and ms > 0
+        ctx.run_prepared()
+        ctx.wait()
+        assert ctx.read_results() == want
+        assert (tmp_path / "tune.txt").exists()
+        t2, c2, ms2 = ctx.autotune(pos)              # served from the cache
+        assert (t2, c2, ms2) == (tile, ctas, -1.0)
