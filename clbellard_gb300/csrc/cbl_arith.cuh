@@ -19,7 +19,7 @@
 //   middle width 1 (2^28 <= m < 2^31): R = 2^32, residues in [0, m).
 //   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m), carries kept.
 //   short width 2 (2^32 <= m < 2^40): R = 2^64, residues in [0, 4m).
-//   width 2 (2^28 <= m < 2^50): R = 2^64 by two word steps, residues in [0, 4m).
+//   width 2 (2^28 <= m < 2^60): R = 2^64 by two word steps, residues in [0, 4m).
 // The ladder step is y <- REDC(y^2) << b with b the next exponent bit; in the
 // lazy kinds 16m < R keeps the result below 4m with no conditional subtraction.
 #pragma once
@@ -84,14 +84,14 @@ __device__ __forceinline__ uint32_t w1s_start(uint32_t m)
     return (uint32_t)r;
 }
 
-// Width 2 (2^28 <= m < 2^50): a value in (0, 2m) congruent to 2^65.
+// Width 2 (2^28 <= m < 2^60): a value in (0, 2m) congruent to 2^65.
 __device__ __forceinline__ uint64_t w2_start(uint64_t m)
 {
     const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
     const float fm = __fmaf_rn(__uint2float_rn(m1), 4294967296.0f, __uint2float_rn(m0));
     const float inv = rcp_approx(fm);
-    const uint64_t q1 = float_to_u64_trunc(36893488147419103232.0f * inv);   // 2^65 / m
-    const int64_t r1 = (int64_t)(0ull - q1 * m);                               // |r1| <= 2^44 + m
+    const uint64_t q1 = float_to_u64_trunc(36893488147419103232.0f * inv);   // 2^65 / m >= 2^5
+    const int64_t r1 = (int64_t)(0ull - q1 * m);                               // |r1| <= 2^44 + m < 2^61
     const float fr1 = __fmaf_rn(__int2float_rn((int32_t)(r1 >> 32)), 4294967296.0f,
                                 __uint2float_rn((uint32_t)r1));
     const int32_t q2 = __float2int_rn(fr1 * inv);                             // |r1/m| <= 2^16 + 1
@@ -284,14 +284,15 @@ __device__ __forceinline__ uint32_t w1m_pow2(uint64_t E, uint32_t m, uint32_t mp
 }
 
 // ---------------------------------------------------------------- width 2 --
-// y = (y0,y1) in [0,4m), m = (m0,m1) with 2^28 <= m < 2^50:
-// REDC_2^64(y^2) << b by two 32-bit word steps, again in [0,4m).
+// y = (y0,y1) in [0,4m), m = (m0,m1) with 2^28 <= m < 2^60 (so y1 < 2^30,
+// m1 < 2^28, T + U m < 2^125): REDC_2^64(y^2) << b by two 32-bit word steps,
+// again in [0,4m) because 16m < 2^64.
 __device__ __forceinline__ void w2_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0, uint32_t m1,
                                        uint32_t mp, uint32_t b)
 {
-    // T = y^2 = t0 + t1 2^32 + t2 2^64 + t3 2^96  (< 16 m^2 < 2^104)
+    // T = y^2 = t0 + t1 2^32 + t2 2^64 + t3 2^96  (< 16 m^2 < 2^124)
     const uint64_t a = (uint64_t)y0 * y0;
-    const uint64_t p = (uint64_t)y0 * (y1 << 1);        // y1 < 2^20
+    const uint64_t p = (uint64_t)y0 * (y1 << 1);        // y1 < 2^30
     const uint64_t s = (uint64_t)y1 * y1;
     const uint32_t t0 = (uint32_t)a;
     uint32_t t1, t2, t3;
@@ -325,7 +326,7 @@ struct W2State {
     __device__ __forceinline__ void step(uint32_t b) { w2_sqr(y0, y1, m0, m1, mp, b); }
 };
 
-// r6 = 2^E mod m in [0, m) for E >= 65 (2^28 <= m < 2^50).
+// r6 = 2^E mod m in [0, m) for E >= 65 (2^28 <= m < 2^60).
 __device__ __forceinline__ uint64_t w2_pow2(uint64_t E, uint64_t m, uint32_t mp)
 {
     const uint64_t y = w2_start(m);

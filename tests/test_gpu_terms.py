@@ -69,9 +69,10 @@ def test_terms_sampled_1e8(ctx192, oracle):
         check_terms(ctx192, oracle, d, f, ks)
 
 
-@pytest.mark.parametrize("d", [3999999999, 39999999999, 399999999999])
+@pytest.mark.parametrize("d", [3999999999, 39999999999, 399999999999, 399999999999999, 39999999999999999,
+                               115000000000000000])
 def test_terms_sampled_large(ctx192, oracle, d):
-    """Positions 1e10 .. 1e12: moduli up to ~2^42, exponents up to ~2^42."""
+    """Positions 1e10 .. 2.9e17: moduli up to just below 2^60, exponents up to ~2^60."""
     rng = random.Random(d)
     for f in range(7):
         ks = [rng.randrange(0, d) for _ in range(3000)] + [d - 1, d - 2, d, d + 19]
@@ -80,5 +81,14 @@ def test_terms_sampled_large(ctx192, oracle, d):
 
 def test_terms_reject_modulus_range(ctx192, cbl):
     with pytest.raises(cbl.CblError) as e:
-        ctx192.terms(1 << 60, 0, [1 << 49])
+        ctx192.terms(1 << 62, 0, [1 << 59])         # 4k + 1 >= 2^60
     assert e.value.code == -6
+
+
+def test_position_limits(ctx192, ctxdd, cbl):
+    with pytest.raises(cbl.CblError) as e:
+        ctx192.compute(999999999999999995)          # moduli reach ~2^61.8
+    assert e.value.code == -2
+    with pytest.raises(cbl.CblError) as e:
+        ctxdd.compute(10 ** 16)                      # mode 0 stops at moduli 2^53
+    assert e.value.code == -2
