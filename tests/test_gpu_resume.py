@@ -53,3 +53,19 @@ def test_graph_replay_equals_direct_launch(ctx192):
     assert ctx192.kernel_ms() > 0.0                  # events inside the replayed graph
     assert ctx192.read_results() == direct
     assert "%048x" % direct[1] == load_golden("oracle_small.json")["1000000"]["hex192"]
+
+
+def test_wait_times_out_then_completes(ctx192, cbl):
+    """cbl_wait with a short limit returns CBL_E_TIMEOUT while a pass is still
+    running (host-side timeout; nothing on the GPU waits), and the pass then
+    completes normally."""
+    ctx192.prepare([10 ** 10])
+    ctx192.run_prepared()
+    with pytest.raises(cbl.CblError) as e:
+        ctx192.wait(1)
+    assert e.value.code == -5
+    assert ctx192.query() == 1
+    ctx192.wait(120000)
+    assert ctx192.query() == 0
+    pub = load_golden("published_digits.json")["digits"]
+    assert ("%048x" % ctx192.read_results()[0]).startswith(pub["10000000000"])
