@@ -14,12 +14,13 @@
 // (exact division by the odd m), so q_j is the Montgomery multiplier of the
 // step and no division is ever executed. The chain ends at r_0 = 2^(10e) mod m.
 //
-// Five residue kinds:
+// Six residue kinds:
 //   width 1 (m < 2^28): R = 2^32, residues kept lazily in [0, 4m).
 //   middle width 1 (2^28 <= m < 2^31): R = 2^32, residues in [0, m).
 //   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m), carries kept.
 //   short width 2 (2^32 <= m < 2^40): R = 2^64, residues in [0, 4m).
 //   width 2 (2^28 <= m < 2^60): R = 2^64 by two word steps, residues in [0, 4m).
+//   wide width 2 (2^60 <= m < 2^62): the same steps with residues in [0, 2m).
 // The ladder step is y <- REDC(y^2) << b with b the next exponent bit; in the
 // lazy kinds 16m < R keeps the result below 4m with no conditional subtraction.
 #pragma once
@@ -84,7 +85,7 @@ __device__ __forceinline__ uint32_t w1s_start(uint32_t m)
     return (uint32_t)r;
 }
 
-// Width 2 (2^28 <= m < 2^60): a value in (0, 2m) congruent to 2^65.
+// Width 2 (2^28 <= m < 2^62): a value in (0, 2m) congruent to 2^65.
 __device__ __forceinline__ uint64_t w2_start(uint64_t m)
 {
     const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
@@ -429,6 +430,34 @@ __device__ __forceinline__ uint64_t w2s_pow2(uint64_t E, uint64_t m, uint32_t mp
     }
     uint64_t r = ((uint64_t)st.y1 << 32) | st.y0;
     r = min(r, r - 2 * m);
+    r = min(r, r - m);
+    return r;
+}
+
+// ------------------------------------------------------- width 2, m >= 2^60 --
+// 2^60 <= m < 2^62 (positions up to 999999999999999999): residues in [0, 2m).
+// REDC(y^2) < 4m^2/2^64 + m < 2m still holds and T + U m < 2^127, so the
+// two-word step of w2_sqr applies; only the doubling needs min(y, y - 2m).
+struct W2XState {
+    uint32_t y0, y1, m0, m1, mp;
+    uint64_t m2;                                        // 2m
+    __device__ __forceinline__ void step(uint32_t b)
+    {
+        w2_sqr(y0, y1, m0, m1, mp, b);                  // < 4m < 2^64
+        uint64_t y = ((uint64_t)y1 << 32) | y0;
+        y = min(y, y - m2);                             // < 2m
+        y0 = (uint32_t)y;
+        y1 = (uint32_t)(y >> 32);
+    }
+};
+
+// r6 = 2^E mod m in [0, m) for E >= 65, 2^28 <= m < 2^62.
+__device__ __forceinline__ uint64_t w2x_pow2(uint64_t E, uint64_t m, uint32_t mp)
+{
+    const uint64_t y = w2_start(m);                     // (0, 2m)
+    W2XState st{(uint32_t)y, (uint32_t)(y >> 32), (uint32_t)m, (uint32_t)(m >> 32), mp, 2 * m};
+    walk_bits(E - 64, st);
+    uint64_t r = ((uint64_t)st.y1 << 32) | st.y0;
     r = min(r, r - m);
     return r;
 }

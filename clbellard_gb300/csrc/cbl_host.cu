@@ -151,20 +151,21 @@ bool series_ok(uint64_t den0, uint64_t den1)
 }
 
 // Append the segments covering k in [k0, k1) of one series, split at d (main
-// vs tail) and at the residue-kind boundaries m = 2^28, 2^31, 2^32 and 2^40. k = 0 with
+// vs tail) and at the residue-kind boundaries m = 2^28, 2^31, 2^32, 2^40 and 2^60. k = 0 with
 // den1 = 1 (m = 1) contributes exactly 0 and is left out.
 int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, int sign, uint32_t slot,
                  uint64_t k0, uint64_t k1)
 {
     if (k0 == 0 && den1 == 1) k0 = 1;
     if (k1 <= k0) return CBL_OK;
-    if ((u128)den0 * (k1 - 1) + den1 >= (u128)kW2Max) return CBL_E_POSITION;
+    if ((u128)den0 * (k1 - 1) + den1 >= (u128)kW2XMax) return CBL_E_POSITION;
     const uint64_t kw1 = (kW1Max - den1 + den0 - 1) / den0;    // first k with m >= 2^28
     const uint64_t kw1m = (kW1MMax - den1 + den0 - 1) / den0;  // first k with m >= 2^31
     const uint64_t kw1s = (kW1SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^32
     const uint64_t kw2s = (kW2SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^40
+    const uint64_t kw2 = (kW2Max - den1 + den0 - 1) / den0;    // first k with m >= 2^60
     std::vector<uint64_t> pts = {k0, k1};
-    for (uint64_t c : {d, kw1, kw1m, kw1s, kw2s}) pts.push_back(std::min(std::max(c, k0), k1));
+    for (uint64_t c : {d, kw1, kw1m, kw1s, kw2s, kw2}) pts.push_back(std::min(std::max(c, k0), k1));
     std::sort(pts.begin(), pts.end());
     for (size_t i = 0; i + 1 < pts.size(); ++i) {
         const uint64_t a = pts[i], b = pts[i + 1];
@@ -176,17 +177,18 @@ int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, 
         s.den0 = den0;
         s.den1 = den1;
         s.slot = slot;
-        s.flags = seg_flags(sign, a >= kw2s ? 2 : (a >= kw1s ? 4 : (a >= kw1m ? 3 : (a >= kw1 ? 5 : 1))));
+        s.flags = seg_flags(sign, a >= kw2 ? 6 : a >= kw2s ? 2 : (a >= kw1s ? 4 : (a >= kw1m ? 3 : (a >= kw1 ? 5 : 1))));
         v.push_back(s);
     }
     return CBL_OK;
 }
 
-// Cost rank of a residue kind: width 2 > short width 2 > strict width 1 >
-// middle width 1 > width 1.
+// Cost rank of a residue kind: wide width 2 > width 2 > short width 2 >
+// strict width 1 > middle width 1 > width 1.
 int kind_rank(uint32_t flags)
 {
     switch ((flags >> 4) & 15u) {
+    case 6: return 5;
     case 2: return 4;
     case 4: return 3;
     case 3: return 2;
@@ -331,7 +333,7 @@ const char *cbl_strerror(int code)
     case CBL_SKIPPED: return "job skipped: k_start > d";
     case CBL_E_ARG: return "invalid argument";
     case CBL_E_POSITION:
-        return "invalid position (outside [5, 999999999999999999], a modulus >= 2^60, or >= 2^53 in mode 0)";
+        return "invalid position (outside [5, 999999999999999999], or a modulus >= 2^53 in mode 0)";
     case CBL_E_NODEVICE: return "no CUDA device";
     case CBL_E_CUDA: return "CUDA runtime error";
     case CBL_E_TIMEOUT: return "timed out waiting for the device";
@@ -516,7 +518,7 @@ int cbl_Sglobal32mtg(cbl_ctx *c, uint64_t offset, uint64_t d, uint64_t k_max, in
 int cbl_Sglobal64mtg(cbl_ctx *c, uint64_t offset, uint64_t d, uint64_t k_max, int64_t numesign, uint64_t den0,
                      uint64_t den1)
 {
-    return sglobal(c, offset, d, k_max, numesign, den0, den1, kW2Max);
+    return sglobal(c, offset, d, k_max, numesign, den0, den1, kW2XMax);
 }
 
 int cbl_Sglobal_after(cbl_ctx *c, uint64_t d, int64_t numesign, uint64_t den0, uint64_t den1)
@@ -932,7 +934,7 @@ int cbl_terms(cbl_ctx *c, uint64_t d, int f, const uint64_t *k, int n, uint64_t 
     if (!c || !formula_ok(f) || n < 0 || (n > 0 && (!k || !out3n))) return CBL_E_ARG;
     if (n == 0) return CBL_OK;
     for (int i = 0; i < n; ++i)
-        if ((u128)kDen0[f] * k[i] + kDen1[f] >= (u128)kW2Max) return CBL_E_RANGE;
+        if ((u128)kDen0[f] * k[i] + kDen1[f] >= (u128)kW2XMax) return CBL_E_RANGE;
     cudaSetDevice(c->device);
     if (n > c->kbuf_cap) {
         cudaFree(c->d_kbuf);

@@ -18,7 +18,8 @@ constexpr uint64_t kW1Max = 1ull << 28;   // width 1 (one 32-bit word) for m < 2
 constexpr uint64_t kW1MMax = 1ull << 31;  // middle width 1 for 2^28 <= m < 2^31
 constexpr uint64_t kW1SMax = 1ull << 32;  // strict width 1 for 2^31 <= m < 2^32
 constexpr uint64_t kW2SMax = 1ull << 40;  // short width 2 for 2^32 <= m < 2^40
-constexpr uint64_t kW2Max = 1ull << 60;   // width 2 (two words) for m < 2^60
+constexpr uint64_t kW2Max = 1ull << 60;   // width 2 (two words, residues < 4m) for m < 2^60
+constexpr uint64_t kW2XMax = 1ull << 62;  // wide width 2 (residues < 2m) for 2^60 <= m < 2^62
 constexpr uint64_t kDDMax = 1ull << 53;   // double-double mode: m and r exact as doubles
 
 constexpr int kTail192 = 20;   // tail terms k = d..d+19 (Bellard.cl:1164-1239)
@@ -33,7 +34,7 @@ struct Seg {
     uint64_t tile0;
     uint32_t den0, den1;
     uint32_t slot;         // accumulator slot (6 x u64 digit sums)
-    uint32_t flags;        // bit 0: series sign (1 = minus), bits 4-7: residue kind 1..5
+    uint32_t flags;        // bit 0: series sign (1 = minus), bits 4-7: residue kind 1..6
 };
 static_assert(sizeof(Seg) == 48, "Seg layout");
 

@@ -50,7 +50,7 @@ __device__ __forceinline__ void shr192(uint32_t q[6], int s)
 // tail value 2^(-10(k-d))/m (digits of 1/m shifted right by 10(k-d)).
 // KIND: 1 = width 1 (m < 2^28), 5 = middle width 1 (2^28 <= m < 2^31),
 // 3 = strict width 1 (2^28 <= m < 2^32), 4 = short width 2 (2^32 <= m < 2^40),
-// 2 = width 2 (2^28 <= m < 2^50).
+// 2 = width 2 (2^28 <= m < 2^60), 6 = wide width 2 (2^60 <= m < 2^62).
 template <int KIND, bool TAIL>
 __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, uint32_t q[6])
 {
@@ -67,6 +67,9 @@ __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, 
         w1_digits(r6, (uint32_t)m, mp, q);
     } else if (KIND == 4) {
         const uint64_t r6 = w2s_pow2(E, m, mp);
+        w2_digits(r6, m, mp, q);
+    } else if (KIND == 6) {
+        const uint64_t r6 = w2x_pow2(E, m, mp);
         w2_digits(r6, m, mp, q);
     } else {
         const uint64_t r6 = w2_pow2(E, m, mp);
@@ -156,12 +159,14 @@ __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restri
             else if (width == 5) run_tile<5, true>(s, kb, ke, lane, acc, cnt);
             else if (width == 3) run_tile<3, true>(s, kb, ke, lane, acc, cnt);
             else if (width == 4) run_tile<4, true>(s, kb, ke, lane, acc, cnt);
+            else if (width == 6) run_tile<6, true>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, true>(s, kb, ke, lane, acc, cnt);
         } else {
             if (width == 1) run_tile<1, false>(s, kb, ke, lane, acc, cnt);
             else if (width == 5) run_tile<5, false>(s, kb, ke, lane, acc, cnt);
             else if (width == 3) run_tile<3, false>(s, kb, ke, lane, acc, cnt);
             else if (width == 4) run_tile<4, false>(s, kb, ke, lane, acc, cnt);
+            else if (width == 6) run_tile<6, false>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, false>(s, kb, ke, lane, acc, cnt);
         }
         // Every k of this lane has the parity of kb + lane: sign (-1)^(k + sign).
@@ -305,13 +310,15 @@ __global__ void terms_each_kernel(uint64_t d, uint32_t den0, uint32_t den1, int 
             else if (m < kW1MMax) term_digits<5, false>(d, k, m, q);
             else if (m < kW1SMax) term_digits<3, false>(d, k, m, q);
             else if (m < kW2SMax) term_digits<4, false>(d, k, m, q);
-            else term_digits<2, false>(d, k, m, q);
+            else if (m < kW2Max) term_digits<2, false>(d, k, m, q);
+            else term_digits<6, false>(d, k, m, q);
         } else {
             if (m < kW1Max) term_digits<1, true>(d, k, m, q);
             else if (m < kW1MMax) term_digits<5, true>(d, k, m, q);
             else if (m < kW1SMax) term_digits<3, true>(d, k, m, q);
             else if (m < kW2SMax) term_digits<4, true>(d, k, m, q);
-            else term_digits<2, true>(d, k, m, q);
+            else if (m < kW2Max) term_digits<2, true>(d, k, m, q);
+            else term_digits<6, true>(d, k, m, q);
         }
         if ((k + (uint64_t)sign) & 1ull)
             for (int j = 0; j < 6; ++j) q[j] = ~q[j];

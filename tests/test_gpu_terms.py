@@ -70,9 +70,10 @@ def test_terms_sampled_1e8(ctx192, oracle):
 
 
 @pytest.mark.parametrize("d", [3999999999, 39999999999, 399999999999, 399999999999999, 39999999999999999,
-                               115000000000000000])
+                               115000000000000000, 399999999999999997])
 def test_terms_sampled_large(ctx192, oracle, d):
-    """Positions 1e10 .. 2.9e17: moduli up to just below 2^60, exponents up to ~2^60."""
+    """Positions 1e10 .. 999999999999999995 (the reference's largest): moduli
+    up to ~2^61.8, exponents up to ~2^62."""
     rng = random.Random(d)
     for f in range(7):
         ks = [rng.randrange(0, d) for _ in range(3000)] + [d - 1, d - 2, d, d + 19]
@@ -81,13 +82,22 @@ def test_terms_sampled_large(ctx192, oracle, d):
 
 def test_terms_reject_modulus_range(ctx192, cbl):
     with pytest.raises(cbl.CblError) as e:
-        ctx192.terms(1 << 62, 0, [1 << 59])         # 4k + 1 >= 2^60
+        ctx192.terms(1 << 63, 0, [1 << 60])         # 4k + 1 >= 2^62
     assert e.value.code == -6
+
+
+@pytest.mark.parametrize("f", range(7))
+def test_terms_60bit_boundary(ctx192, oracle, f):
+    """k around the first modulus >= 2^60 (width 2 -> wide width 2)."""
+    den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
+    k60 = ((1 << 60) - den1 + den0 - 1) // den0
+    d = 399999999999999997
+    check_terms(ctx192, oracle, d, f, list(range(k60 - 40, k60 + 40)) + list(range(d - 40, d + 20)))
 
 
 def test_position_limits(ctx192, ctxdd, cbl):
     with pytest.raises(cbl.CblError) as e:
-        ctx192.compute(999999999999999995)          # moduli reach ~2^61.8
+        ctx192.compute(10 ** 18)                     # above the reference's limit
     assert e.value.code == -2
     with pytest.raises(cbl.CblError) as e:
         ctxdd.compute(10 ** 16)                      # mode 0 stops at moduli 2^53
