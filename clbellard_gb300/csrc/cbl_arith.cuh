@@ -164,38 +164,20 @@ __device__ __forceinline__ uint32_t w1_digits(uint32_t r, uint32_t m, uint32_t m
 }
 
 // --------------------------------------------------------- strict width 1 --
-// 2^28 <= m < 2^32: R = 2^32 with residues in [0, m). REDC(y^2) < 2m needs one
-// conditional subtraction (with the carry out of bit 32), and so does 2y.
+// 2^31 <= m < 2^32: R = 2^32, residues in [0, m). u m + y^2 can pass 2^64
+// once: the multiply-add takes y^2 as its addend and the wrapped carry c is
+// recovered by comparing high words; REDC = x + c 2^32 < 2m. The doubling's
+// carry out of bit 31 comes from a funnel shift. (Valid for 2^28 <= m < 2^32.)
 __device__ __forceinline__ uint32_t w1s_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
 {
     const uint64_t t = (uint64_t)y * y;
-    const uint32_t t0 = (uint32_t)t, t1 = (uint32_t)(t >> 32);
-    const uint32_t u = t0 * mp;
-    const uint64_t v = (uint64_t)u * m;
-    uint32_t z, c;
-    asm("add.cc.u32 %0, %2, %3;\n\t"                   // carry = (t0 != 0): t0 + lo(um) = 0 mod 2^32
-        "addc.cc.u32 %0, %4, %5;\n\t"
-        "addc.u32 %1, 0, 0;"
-        : "=r"(z), "=r"(c)
-        : "r"(t0), "r"((uint32_t)v), "r"(t1), "r"((uint32_t)(v >> 32)));
-    uint32_t zm, bw;                                    // (c:z) - m, borrow-extended
-    asm("sub.cc.u32 %0, %2, %3;\n\t"
-        "subc.u32 %1, %4, 0;"
-        : "=r"(zm), "=r"(bw)
-        : "r"(z), "r"(m), "r"(c));
-    z = bw ? z : zm;
-    const uint32_t dd = z & (0u - b);                   // doubling when b
-    uint32_t z2, c2;
-    asm("add.cc.u32 %0, %2, %3;\n\t"
-        "addc.u32 %1, 0, 0;"
-        : "=r"(z2), "=r"(c2)
-        : "r"(z), "r"(dd));
-    uint32_t z2m, bw2;
-    asm("sub.cc.u32 %0, %2, %3;\n\t"
-        "subc.u32 %1, %4, 0;"
-        : "=r"(z2m), "=r"(bw2)
-        : "r"(z2), "r"(m), "r"(c2));
-    return bw2 ? z2 : z2m;
+    const uint32_t t1 = (uint32_t)(t >> 32);
+    const uint32_t u = (uint32_t)t * mp;
+    const uint32_t x = (uint32_t)(((uint64_t)u * m + t) >> 32);   // (t1 + h) mod 2^32
+    const uint32_t r = (x < t1) ? x - m : min(x, x - m);          // REDC mod m, in [0, m)
+    const uint32_t x2 = r << b;
+    const uint32_t c2 = __funnelshift_l(r, 0u, b);                 // bit shifted out of r
+    return c2 ? x2 - m : min(x2, x2 - m);                          // 2^b r mod m
 }
 
 struct W1SState {
