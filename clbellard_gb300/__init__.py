@@ -14,7 +14,7 @@ import os
 
 from . import build as _build
 
-__all__ = ["Context", "CblError", "load", "pos_to_d", "workmode_sum", "formula", "library_path",
+__all__ = ["Context", "CblError", "load", "pos_to_d", "workmode_sum", "formula", "library_path", "plan_jobs",
            "BATCHSIZE", "SKIPPED"]
 
 BATCHSIZE = 137438953472          # 2^37 k-values per work-mode job (Bellard_192.hsp:19)
@@ -71,6 +71,8 @@ def load(build_if_missing: bool = True):
         "cbl_compute": ([vp, u64, ctypes.c_char_p], c_int),
         "cbl_compute_hexpos": ([vp, u64, ctypes.c_char_p], c_int),
         "cbl_run_job": ([vp, u64, c_int, u64, u64, ctypes.c_char_p], c_int),
+        "cbl_run_job_range": ([vp, u64, c_int, u64, u64, ctypes.c_char_p], c_int),
+        "cbl_plan_jobs": ([u64, c_int, ctypes.POINTER(c_int), P64, P64, c_int], c_int),
         "cbl_workmode_sum": ([ctypes.POINTER(ctypes.c_char_p), c_int, ctypes.c_char_p], c_int),
         "cbl_job_write": ([ctypes.c_char_p, c_int, u64, ctypes.c_char_p, c_int, ctypes.c_char_p, i64], c_int),
         "cbl_job_read": ([ctypes.c_char_p, c_int, u64, ctypes.c_char_p], c_int),
@@ -136,6 +138,16 @@ def workmode_sum(hexes) -> str:
     out = ctypes.create_string_buffer(49)
     _check(L.cbl_workmode_sum(arr, len(hexes), out), "cbl_workmode_sum")
     return out.value.decode()
+
+
+def plan_jobs(needD: int, njobs: int):
+    """Balanced work-mode jobs: [(s, k0, k1)] of about equal estimated cost."""
+    L = load()
+    S = (ctypes.c_int * njobs)()
+    K0 = (ctypes.c_uint64 * njobs)()
+    K1 = (ctypes.c_uint64 * njobs)()
+    n = _check(L.cbl_plan_jobs(needD, njobs, S, K0, K1, njobs), "cbl_plan_jobs")
+    return [(S[i], K0[i], K1[i]) for i in range(n)]
 
 
 def words_to_int(w) -> int:
@@ -255,6 +267,12 @@ class Context:
         """Hex of job (s, b), or None when the reference would skip it."""
         out = ctypes.create_string_buffer(49)
         rc = _check(load().cbl_run_job(self._h, needD, s, b, batchsize, out), "run_job")
+        return None if rc == SKIPPED else out.value.decode()
+
+    def run_job_range(self, needD: int, s: int, k0: int, k1: int):
+        """Hex of a job over k in [k0, k1) of series s, or None if k0 > d."""
+        out = ctypes.create_string_buffer(49)
+        rc = _check(load().cbl_run_job_range(self._h, needD, s, k0, k1, out), "run_job_range")
         return None if rc == SKIPPED else out.value.decode()
 
     def batch(self, positions):

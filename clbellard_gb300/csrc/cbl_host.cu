@@ -829,6 +829,130 @@ int cbl_run_job(cbl_ctx *c, uint64_t needD, int s, uint64_t b, uint64_t batchsiz
     return rc;
 }
 
+// ---- balanced work-mode planning
+// Relative cost of one ladder step per residue kind (instructions per step
+// measured with ncu on GB300: about 7, 10, 13, 25, 28, 30).
+static double step_cost(uint64_t m)
+{
+    if (m < kW1Max) return 7.0;
+    if (m < kW1MMax) return 10.0;
+    if (m < kW1SMax) return 13.0;
+    if (m < kW2SMax) return 25.0;
+    if (m < kW2Max) return 28.0;
+    return 30.0;
+}
+
+// Estimated cost of terms k in [k0, k1) of series f at position d (k < d):
+// (bitlen(10(d - k)) + 8) steps per term (the 8 stands for the start value and
+// the six digit steps) times the kind's step cost; piecewise constant between
+// the powers of two of 10(d - k) and the kind boundaries.
+static double range_cost(uint64_t d, int f, uint64_t k0, uint64_t k1)
+{
+    const uint64_t den0 = kDen0[f], den1 = kDen1[f];
+    double total = 0.0;
+    uint64_t k = k0;
+    while (k < k1) {
+        const uint64_t e10 = 10 * (d - k);
+        const int bl = 64 - __builtin_clzll(e10);
+        // next k where bitlen(10(d-k)) drops: 10(d-k) < 2^(bl-1)  <=>  k > d - 2^(bl-1)/10
+        const uint64_t lim = (uint64_t)1 << (bl - 1);
+        uint64_t knext = d - (lim - 1) / 10;                 // first k with 10(d-k) < 2^(bl-1)
+        if (knext <= k) knext = k + 1;
+        const uint64_t m = den0 * k + den1;
+        const uint64_t bounds[5] = {kW1Max, kW1MMax, kW1SMax, kW2SMax, kW2Max};
+        for (uint64_t b : bounds)
+            if (m < b) {
+                const uint64_t kb = (b - den1 + den0 - 1) / den0;
+                if (kb < knext) knext = kb;
+                break;
+            }
+        if (knext > k1) knext = k1;
+        if (knext <= k) knext = k + 1;
+        total += (double)(knext - k) * (bl + 8) * step_cost(m);
+        k = knext;
+    }
+    return total;
+}
+
+int cbl_plan_jobs(uint64_t needD, int njobs, int *out_s, uint64_t *out_k0, uint64_t *out_k1, int cap)
+{
+    if (njobs < 7 || cap < njobs || !out_s || !out_k0 || !out_k1) return CBL_E_ARG;
+    uint64_t d;
+    int rc = cbl_pos_to_d(needD, &d, nullptr);
+    if (rc) return rc;
+    double cost[7], total = 0;
+    for (int f = 0; f < 7; ++f) total += cost[f] = range_cost(d, f, 0, d) + 1.0;
+    // jobs per series in proportion to its cost, at least one each
+    int per[7], used = 0;
+    // (at most d jobs per series: each job keeps at least one term below d)
+    const int maxper = (int)std::min<uint64_t>(d, (uint64_t)njobs);
+    for (int f = 0; f < 7; ++f) {
+        per[f] = std::min(maxper, std::max(1, (int)(njobs * cost[f] / total)));
+        used += per[f];
+    }
+    while (used > njobs) {
+        int f = (int)(std::max_element(per, per + 7) - per);
+        --per[f];
+        --used;
+    }
+    while (used < njobs) {                                  // give the rest to the heaviest cost per job
+        int best = -1;
+        for (int f = 0; f < 7; ++f)
+            if (per[f] < maxper && (best < 0 || cost[f] / per[f] > cost[best] / per[best])) best = f;
+        if (best < 0) break;
+        ++per[best];
+        ++used;
+    }
+    int n = 0;
+    for (int f = 0; f < 7; ++f) {
+        uint64_t k = 0;
+        for (int j = 0; j < per[f]; ++j) {
+            uint64_t kend = d;
+            if (j + 1 < per[f]) {                           // cost target by bisection on k
+                const double target = cost[f] * (j + 1) / per[f];
+                uint64_t lo = k, hi = d;
+                while (lo + 1 < hi) {
+                    const uint64_t mid = lo + (hi - lo) / 2;
+                    if (range_cost(d, f, 0, mid) < target) lo = mid; else hi = mid;
+                }
+                // a job that reaches d also runs the tail (cbl_BatchCalc), so all
+                // but the last job of a series end below d, each with >= 1 term
+                kend = std::min(std::max(hi, k + 1), d - (uint64_t)(per[f] - 1 - j));
+            }
+            out_s[n] = f;
+            out_k0[n] = k;
+            out_k1[n] = j + 1 < per[f] ? kend : d + kTail192;   // the last job of a series takes the tail
+            ++n;
+            k = kend;
+        }
+    }
+    return n;
+}
+
+int cbl_run_job_range(cbl_ctx *c, uint64_t needD, int s, uint64_t k0, uint64_t k1, char hex[49])
+{
+    if (!c || !hex || !formula_ok(s) || k1 < k0) return CBL_E_ARG;
+    uint64_t d;
+    int rc = cbl_pos_to_d(needD, &d, nullptr);
+    if (rc) return rc;
+    if (k0 > d) return CBL_SKIPPED;
+    cudaSetDevice(c->device);
+    rc = cbl_Set0mem(c);
+    if (!rc) rc = cbl_BatchCalc(c, k0, k1, s, d);
+    if (!rc) rc = cbl_AddAns(c, s);
+    if (rc) return rc;
+    if (is192(c)) {
+        uint64_t w[3];
+        rc = cbl_read_partial(c, w);
+        if (!rc) to_hex192(w, hex);
+    } else {
+        double a[2];
+        rc = cbl_read_partial(c, a);
+        if (!rc) dd_to_hex(a[0], a[1], hex);
+    }
+    return rc;
+}
+
 int cbl_workmode_sum(const char *const *hex48, int n, char out[49])
 {
     if (!out || n < 0 || (n > 0 && !hex48)) return CBL_E_ARG;

@@ -7,6 +7,7 @@
  *   cbl work   <worklist.txt> [workdir] [device]
  *   cbl sum    [workdir]
  *   cbl hexpos <p> [device]            any hex position p >= 3
+ *   cbl plan   <digits> <jobs> [precision]   balanced worklist on stdout
  */
 #include <ctype.h>
 #include <stdint.h>
@@ -98,14 +99,17 @@ static int cmd_work(int argc, char **argv)
             }
             cbl_device_name(c, name, sizeof name);
         } else {
-            /* "s_b" (Bellard_192.hsp:238-244) */
+            /* "s_b" (Bellard_192.hsp:238-244), or "s_b k0 k1" for an explicit k-range */
             if (!isdigit((unsigned char)line[0]) || line[1] != '_') { ++ln; continue; }
             int s = line[0] - '0';
-            uint64_t b = strtoull(line + 2, NULL, 10);
+            char *end = NULL;
+            uint64_t b = strtoull(line + 2, &end, 10);
+            unsigned long long k0 = 0, k1 = 0;
+            const int ranged = end && sscanf(end, "%llu %llu", &k0, &k1) == 2;
             char hex[49];
             if (cbl_job_read(workdir, s, b, hex) == CBL_OK) { ++ln; continue; } /* done before (:307-308) */
             const int64_t t0 = now_ms();
-            rc = cbl_run_job(c, needD, s, b, kBatchSize, hex);
+            rc = ranged ? cbl_run_job_range(c, needD, s, k0, k1, hex) : cbl_run_job(c, needD, s, b, kBatchSize, hex);
             const int64_t ms = now_ms() - t0;
             if (rc == CBL_SKIPPED) { ++ln; continue; }
             if (rc) { fclose(f); cbl_destroy(c); return fail(rc, "cbl_run_job"); }
@@ -149,12 +153,34 @@ static int cmd_hexpos(int argc, char **argv)
     return 0;
 }
 
+static int cmd_plan(int argc, char **argv)
+{
+    if (argc < 4) return fprintf(stderr, "usage: cbl plan <digits> <jobs> [precision]\n"), 2;
+    const uint64_t needD = parse_digits(argv[2]);
+    const int njobs = atoi(argv[3]);
+    const int precision = argc > 4 ? atoi(argv[4]) : 1;
+    if (njobs < 7 || njobs > 100000) return fail(CBL_E_ARG, "jobs");
+    int *s = malloc(sizeof(int) * njobs);
+    uint64_t *k0 = malloc(sizeof(uint64_t) * njobs), *k1 = malloc(sizeof(uint64_t) * njobs);
+    int count[7] = {0};
+    const int n = cbl_plan_jobs(needD, njobs, s, k0, k1, njobs);
+    if (n < 0) return free(s), free(k0), free(k1), fail(n, "cbl_plan_jobs");
+    uint64_t adj = 0, d = 0;
+    cbl_pos_to_d(needD, &d, &adj);
+    printf("digits=%llu\nprecision=%d (0=106bit , 1=192bit)\n", (unsigned long long)adj, precision);
+    for (int i = 0; i < n; ++i)
+        printf("%d_%d %llu %llu\n", s[i], count[s[i]]++, (unsigned long long)k0[i], (unsigned long long)k1[i]);
+    free(s); free(k0); free(k1);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     if (argc >= 2 && !strcmp(argv[1], "normal")) return cmd_normal(argc, argv);
     if (argc >= 2 && !strcmp(argv[1], "work")) return cmd_work(argc, argv);
     if (argc >= 2 && !strcmp(argv[1], "sum")) return cmd_sum(argc, argv);
     if (argc >= 2 && !strcmp(argv[1], "hexpos")) return cmd_hexpos(argc, argv);
-    fprintf(stderr, "usage: cbl normal|work|sum|hexpos ...\n");
+    if (argc >= 2 && !strcmp(argv[1], "plan")) return cmd_plan(argc, argv);
+    fprintf(stderr, "usage: cbl normal|work|sum|hexpos|plan ...\n");
     return 2;
 }

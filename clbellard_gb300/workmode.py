@@ -23,6 +23,9 @@ class Worklist:
     digits: int
     precision: int
     jobs: List[Tuple[int, int]] = field(default_factory=list)
+    # explicit k-ranges of balanced jobs: (s, b) -> (k0, k1); jobs without an
+    # entry cover the reference's batch [b * BATCHSIZE, (b + 1) * BATCHSIZE)
+    ranges: dict = field(default_factory=dict)
 
 
 def parse_worklist(text: str) -> Worklist:
@@ -38,18 +41,39 @@ def parse_worklist(text: str) -> Worklist:
     precision = int(pstr[0]) if pstr[:1] in ("0", "1", "2") else -1
     if not (5 <= digits <= MAX_DIGITS) or precision < 0:
         raise ValueError("invalid worklist header (digits=%r precision=%r)" % (lines[0], lines[1]))
-    jobs = []
+    jobs, ranges = [], {}
     for ln in lines[2:]:
-        ln = ln.strip()
-        if len(ln) >= 3 and ln[0].isdigit() and ln[1] == "_" and ln[2:].isdigit():
-            jobs.append((int(ln[0]), int(ln[2:])))
-    return Worklist(digits, precision, jobs)
+        parts = ln.split()
+        if not parts:
+            continue
+        tok = parts[0]
+        if len(tok) >= 3 and tok[0].isdigit() and tok[1] == "_" and tok[2:].isdigit():
+            job = (int(tok[0]), int(tok[2:]))
+            jobs.append(job)
+            # extension: "s_b k0 k1" gives the job an explicit k-range
+            if len(parts) >= 3 and parts[1].isdigit() and parts[2].isdigit():
+                ranges[job] = (int(parts[1]), int(parts[2]))
+    return Worklist(digits, precision, jobs, ranges)
 
 
 def format_worklist(wl: Worklist) -> str:
     out = ["digits=%d" % wl.digits, "precision=%d (0=106bit , 1=192bit)" % wl.precision]
-    out += ["%d_%d" % j for j in wl.jobs]
+    for j in wl.jobs:
+        out.append("%d_%d %d %d" % (j + wl.ranges[j]) if j in wl.ranges else "%d_%d" % j)
     return "\n".join(out) + "\n"
+
+
+def balanced_worklist(needD: int, njobs: int, precision: int = 1) -> Worklist:
+    """njobs jobs of about equal device time (cbl_plan_jobs), numbered per series."""
+    from . import plan_jobs
+    wl = Worklist(needD, precision)
+    count = [0] * 7
+    for s, k0, k1 in plan_jobs(needD, njobs):
+        job = (s, count[s])
+        count[s] += 1
+        wl.jobs.append(job)
+        wl.ranges[job] = (k0, k1)
+    return wl
 
 
 def all_jobs(d: int, batchsize: int = BATCHSIZE) -> List[Tuple[int, int]]:
@@ -96,18 +120,23 @@ def workdir_sum(workdir: str):
 
 
 JobFn = Callable[[int, int, int, int], Optional[str]]   # (needD, s, b, batchsize) -> hex48 | None
+RangeFn = Callable[[int, int, int, int], Optional[str]]  # (needD, s, k0, k1) -> hex48 | None
 
 
 def run_jobs(jobs, needD: int, workdir: str, job_fn: JobFn, batchsize: int = BATCHSIZE, deviceno: int = 0,
-             devname: str = "") -> int:
+             devname: str = "", ranges: Optional[dict] = None, range_fn: Optional[RangeFn] = None) -> int:
     """*Batchloop (Bellard_192.hsp:298-340): run each job not already on disk,
-    write its file. Returns the number of jobs run."""
+    write its file. Jobs listed in `ranges` run over their explicit k-range
+    with range_fn. Returns the number of jobs run."""
     n = 0
     for s, b in jobs:
         if read_job(workdir, s, b) is not None:       # finished earlier (:307-308)
             continue
         t0 = time.time()
-        h = job_fn(needD, s, b, batchsize)
+        if ranges and (s, b) in ranges:
+            h = range_fn(needD, s, *ranges[(s, b)])
+        else:
+            h = job_fn(needD, s, b, batchsize)
         if h is None:                                 # k_start > d (:306)
             continue
         write_job(workdir, s, b, h, deviceno, devname, int((time.time() - t0) * 1000))
@@ -117,6 +146,10 @@ def run_jobs(jobs, needD: int, workdir: str, job_fn: JobFn, batchsize: int = BAT
 
 def gpu_job_fn(ctx: Context) -> JobFn:
     return lambda needD, s, b, bs: ctx.run_job(needD, s, b, bs)
+
+
+def gpu_range_fn(ctx: Context) -> RangeFn:
+    return lambda needD, s, k0, k1: ctx.run_job_range(needD, s, k0, k1)
 
 
 def merge_gathered(parts: Sequence[Sequence[str]]) -> str:

@@ -117,6 +117,16 @@ int cbl_compute_hexpos(cbl_ctx *ctx, uint64_t p, char hex[49]);
  * k in [b*batchsize, (b+1)*batchsize) of series s, weighted by numer; hex is
  * line 0 of the reference's work/<s>/<s>_<b>.txt. CBL_SKIPPED if b*batchsize > d. */
 int cbl_run_job(cbl_ctx *ctx, uint64_t needD, int s, uint64_t b, uint64_t batchsize, char hex[49]);
+/* Work-mode job over an explicit k-range [k0, k1) of series s (the tail is
+ * included when the range reaches d), weighted by numer; as cbl_run_job. */
+int cbl_run_job_range(cbl_ctx *ctx, uint64_t needD, int s, uint64_t k0, uint64_t k1, char hex[49]);
+/* Balanced work-mode plan (instead of the reference's fixed 2^37-term batches,
+ * Bellard_192.hsp:19): njobs >= 7 jobs of about equal estimated device time,
+ * from a per-term model (ladder steps x the residue kind's step cost). Job i is
+ * series out_s[i], k in [out_k0[i], out_k1[i]); the ranges of one series tile
+ * [0, d + 20), and only the last one reaches d. At most d jobs per series.
+ * Returns the number of jobs (<= njobs <= cap) or a negative code. */
+int cbl_plan_jobs(uint64_t needD, int njobs, int *out_s, uint64_t *out_k0, uint64_t *out_k1, int cap);
 /* workmodeSum0_6.hsp:10-49: sum of n 48-digit hex strings mod 16^48. */
 int cbl_workmode_sum(const char *const *hex48, int n, char out[49]);
 /* Write / read a job file in the reference layout (Bellard_192.hsp:514-533):

@@ -40,6 +40,19 @@ def test_work_mode_and_merge(tmp_path):
     assert "0:1" in out and "6:1" in out
 
 
+def test_plan_then_work(tmp_path):
+    """`cbl plan` writes a balanced worklist that `cbl work` runs and `cbl sum` merges."""
+    plan = subprocess.run([driver(), "plan", "1000000", "14"], capture_output=True, text=True, check=True).stdout
+    lines = plan.splitlines()
+    assert lines[0] == "digits=1000000" and len(lines) == 16
+    wl = tmp_path / "worklist.txt"
+    wl.write_text(plan)
+    work = tmp_path / "work"
+    subprocess.run([driver(), "work", str(wl), str(work)], capture_output=True, text=True, check=True)
+    out = subprocess.run([driver(), "sum", str(work)], capture_output=True, text=True, check=True).stdout
+    assert load_golden("oracle_small.json")["1000000"]["hex192"] in out
+
+
 def test_hexpos():
     out = subprocess.run([driver(), "hexpos", "5"], capture_output=True, text=True, check=True).stdout
     assert out.startswith("6a8885a308d313198a2e0370734")

@@ -103,6 +103,30 @@ def test_workmode_jobs_sum_to_result(ctx192, tmp_path, oracle):
     assert ctx192.run_job(needD, 0, d // bs + 1, bs) is None          # k_start > d: skipped
 
 
+def test_balanced_jobs_sum_to_result(ctx192, tmp_path):
+    """Balanced explicit-range jobs (cbl_plan_jobs) merged equal normal mode."""
+    from clbellard_gb300 import workmode as W
+    needD = 10 ** 7
+    wl = W.balanced_worklist(needD, 20)
+    W.run_jobs(wl.jobs, needD, str(tmp_path), W.gpu_job_fn(ctx192), ranges=wl.ranges,
+               range_fn=W.gpu_range_fn(ctx192), devname=ctx192.device_name)
+    total, counts = W.workdir_sum(str(tmp_path))
+    assert sum(counts) == 20
+    assert total == ctx192.compute(needD) == load_golden("oracle_small.json")[str(needD)]["hex192"]
+
+
+def test_job_range_matches_oracle(ctx192, oracle):
+    needD = 100000
+    d, _ = oracle.pos_to_d(needD)
+    for s, k0, k1 in [(0, 0, 1), (3, 17, 9001), (6, 39000, d), (2, d - 5, d + 20), (5, 0, d + 20)]:
+        kend = min(k1, d)
+        v = oracle.sum_range(d, s, k0, kend, 3) if k0 < kend else 0
+        if max(k0, kend) == d:
+            v += oracle.sum_range(d, s, d, d + 20, 3)
+        assert ctx192.run_job_range(needD, s, k0, k1) == "%048x" % ((v << oracle.NUMER_LOG2[s]) % (1 << 192))
+    assert ctx192.run_job_range(needD, 0, d + 1, d + 20) is None
+
+
 def test_default_batch_jobs(ctx192, oracle):
     """The reference's 2^37 batch: one job per series covers d < 2^37."""
     needD = 10000

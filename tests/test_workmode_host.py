@@ -71,6 +71,70 @@ def test_skip_past_d(cbl, oracle):
     assert fn(10000, 0, d // 1000 + 1, 1000) is None
 
 
+def oracle_range(oracle):
+    """Job partial over an explicit k-range (the tail when the range reaches d)."""
+    def fn(needD, s, k0, k1):
+        d, _ = oracle.pos_to_d(needD)
+        if k0 > d:
+            return None
+        kend = min(k1, d)
+        v = oracle.sum_range(d, s, k0, kend, 3) if k0 < kend else 0
+        if max(k0, kend) == d:
+            v += oracle.sum_range(d, s, d, d + 20, 3)
+        return "%048x" % ((v << oracle.NUMER_LOG2[s]) % (1 << 192))
+    return fn
+
+
+@pytest.mark.parametrize("needD,njobs", [(10, 7), (10, 50), (100000, 16), (10 ** 10, 64), (10 ** 17, 200)])
+def test_plan_tiles_each_series(cbl, oracle, needD, njobs):
+    """Each series' ranges tile [0, d + 20) in order, only the last reaches d."""
+    d, _ = oracle.pos_to_d(needD)
+    plan = cbl.plan_jobs(needD, njobs)
+    assert 7 <= len(plan) <= njobs
+    for s in range(7):
+        rs = [(k0, k1) for f, k0, k1 in plan if f == s]
+        assert rs and rs[0][0] == 0 and rs[-1][1] == d + 20
+        assert all(a[1] == b[0] for a, b in zip(rs, rs[1:]))
+        assert all(k0 < k1 for k0, k1 in rs)
+        assert all(k1 < d for _, k1 in rs[:-1])
+    with pytest.raises(cbl.CblError):
+        cbl.plan_jobs(needD, 6)
+
+
+def test_plan_balances_modelled_cost(cbl, oracle):
+    """Per-term cost model (ladder bits + 8) x kind step cost, summed with
+    numpy over every term: planned jobs are within 10% of each other."""
+    import numpy as np
+    needD = 10 ** 6
+    d, _ = oracle.pos_to_d(needD)
+    den = [(4, 1), (4, 3), (10, 1), (10, 3), (10, 5), (10, 7), (10, 9)]
+    plan = cbl.plan_jobs(needD, 21)
+    costs = []
+    for s, k0, k1 in plan:
+        k = np.arange(k0, min(k1, d), dtype=np.uint64)
+        bits = np.floor(np.log2((10 * (d - k)).astype(np.float64))) + 1
+        m = den[s][0] * k + den[s][1]
+        step = np.where(m < 2 ** 28, 7.0, 10.0)            # m < 4e6 here: the two smallest kinds
+        costs.append(float(((bits + 8) * step).sum()))
+    assert max(costs) / min(costs) < 1.10
+
+
+def test_balanced_worklist_sum_equals_normal_mode(tmp_path, cbl, oracle):
+    """A balanced worklist written, parsed, run and merged gives the normal-mode bits."""
+    from clbellard_gb300 import workmode as W
+    needD = 100000
+    wl = W.balanced_worklist(needD, 12)
+    text = W.format_worklist(wl)
+    assert all(len(ln.split()) == 3 for ln in text.splitlines()[2:])
+    back = W.parse_worklist(text)
+    assert back.jobs == wl.jobs and back.ranges == wl.ranges
+    n = W.run_jobs(back.jobs, needD, str(tmp_path), None, ranges=back.ranges, range_fn=oracle_range(oracle))
+    assert n == len(wl.jobs)
+    total, counts = W.workdir_sum(str(tmp_path))
+    assert sum(counts) == len(wl.jobs)
+    assert total == load_golden("oracle_small.json")["100000"]["hex192"]
+
+
 def test_shard_covers_disjointly():
     from clbellard_gb300 import workmode as W
     jobs = W.all_jobs(10 ** 6, 1000)
