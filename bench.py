@@ -296,8 +296,8 @@ def ours_arm(args):
                      "frac": achieved / (peak_ops / 1e9), "traffic": traffic,
                      "kernel": "terms192_kernel", "kernel_ms": kms,
                      "work": "32-bit multiply halves: 4S+12 per term (m<2^32), 18S+33 (m>=2^32)",
-                     "peak_source": "measured mad.wide.u32 issue rate x 2 halves on this GPU (no integer "
-                                    "peak in MEASURED_PEAKS.json)"},
+                     "peak_source": "measured mad.lo.u32 issue rate (dependent chains, one half each) on this "
+                                    "GPU (no integer peak in MEASURED_PEAKS.json)"},
         "gpu_launches": launches,
         "result_hex": result,
         "clocks": clk.summary(),

@@ -125,14 +125,44 @@ __device__ __forceinline__ void walk_bits(uint64_t Ep, State &st)
     }
 }
 
+// ------------------------------------------------- multiply-add chains --
+// Every REDC word step below is written as a PTX carry chain of mad.lo.cc /
+// madc.hi over 32-bit words. A 64-bit multiply-add (mad.wide with a 64-bit
+// addend) issues more slowly on sm_103a than the two chained halves, and the
+// carry out of the chain comes for free.
+
+// hi(u m + (t0, t1)) mod 2^32, where u m + t0 = 0 mod 2^32 (a REDC word step).
+__device__ __forceinline__ uint32_t redc_word(uint32_t u, uint32_t m, uint32_t t0, uint32_t t1)
+{
+    uint32_t r;
+    asm("{\n\t.reg .u32 x;\n\t"
+        "mad.lo.cc.u32 x, %1, %2, %3;\n\t"
+        "madc.hi.u32 %0, %1, %2, %4;\n\t}"
+        : "=r"(r)
+        : "r"(u), "r"(m), "r"(t0), "r"(t1));
+    return r;
+}
+
+// As redc_word, also returning the carry out of the high word in c (0 or 1).
+__device__ __forceinline__ uint32_t redc_word_c(uint32_t u, uint32_t m, uint32_t t0, uint32_t t1, uint32_t &c)
+{
+    uint32_t r;
+    asm("{\n\t.reg .u32 x;\n\t"
+        "mad.lo.cc.u32 x, %2, %3, %4;\n\t"
+        "madc.hi.cc.u32 %0, %2, %3, %5;\n\t"
+        "addc.u32 %1, 0, 0;\n\t}"
+        : "=r"(r), "=r"(c)
+        : "r"(u), "r"(m), "r"(t0), "r"(t1));
+    return r;
+}
+
 // ---------------------------------------------------------------- width 1 --
 // y in [0,4m), m < 2^28: REDC_2^32(y^2) << b, again in [0,4m).
 __device__ __forceinline__ uint32_t w1_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
 {
     const uint64_t t = (uint64_t)y * y;                 // < 16 m^2 < 2^60
     const uint32_t u = (uint32_t)t * mp;
-    const uint64_t s = (uint64_t)u * m + t;             // low word is 0
-    return (uint32_t)(s >> 32) << b;
+    return redc_word(u, m, (uint32_t)t, (uint32_t)(t >> 32)) << b;   // (t + u m) / 2^32 < 2m
 }
 
 struct W1State {
@@ -158,23 +188,23 @@ __device__ __forceinline__ uint32_t w1_digits(uint32_t r, uint32_t m, uint32_t m
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         q[j] = r * mp;
-        r = (uint32_t)(((uint64_t)q[j] * m + r) >> 32);
+        r = redc_word(q[j], m, r, 0u);                  // (r + q m) / 2^32 < m
     }
     return r;
 }
 
 // --------------------------------------------------------- strict width 1 --
 // 2^31 <= m < 2^32: R = 2^32, residues in [0, m). u m + y^2 can pass 2^64
-// once: the multiply-add takes y^2 as its addend and the wrapped carry c is
-// recovered by comparing high words; REDC = x + c 2^32 < 2m. The doubling's
-// carry out of bit 31 comes from a funnel shift. (Valid for 2^28 <= m < 2^32.)
+// once: the carry chain returns the carry c out of the high word, and
+// REDC = x + c 2^32 < 2m. The doubling's carry out of bit 31 comes from a
+// funnel shift. (Valid for 2^28 <= m < 2^32.)
 __device__ __forceinline__ uint32_t w1s_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
 {
     const uint64_t t = (uint64_t)y * y;
-    const uint32_t t1 = (uint32_t)(t >> 32);
     const uint32_t u = (uint32_t)t * mp;
-    const uint32_t x = (uint32_t)(((uint64_t)u * m + t) >> 32);   // (t1 + h) mod 2^32
-    const uint32_t r = (x < t1) ? x - m : min(x, x - m);          // REDC mod m, in [0, m)
+    uint32_t c;
+    const uint32_t x = redc_word_c(u, m, (uint32_t)t, (uint32_t)(t >> 32), c);
+    const uint32_t r = c ? x - m : min(x, x - m);                  // REDC mod m, in [0, m)
     const uint32_t x2 = r << b;
     const uint32_t c2 = __funnelshift_l(r, 0u, b);                 // bit shifted out of r
     return c2 ? x2 - m : min(x2, x2 - m);                          // 2^b r mod m
@@ -195,13 +225,13 @@ __device__ __forceinline__ uint32_t w1s_pow2(uint64_t E, uint32_t m, uint32_t mp
 
 // ------------------------------------------------------ middle width 1 --
 // 2^28 <= m < 2^31: R = 2^32, residues in [0, m). y^2 + u m < 2^64, so the
-// reduction is one multiply-add with y^2 as its addend and no carry handling;
-// REDC < 2m and the doubling < 2m are brought back below m by min(x, x - m).
+// reduction is one word step with no carry out; REDC < 2m and the doubling
+// < 2m are brought back below m by min(x, x - m).
 __device__ __forceinline__ uint32_t w1m_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
 {
     const uint64_t t = (uint64_t)y * y;
     const uint32_t u = (uint32_t)t * mp;
-    const uint32_t z = (uint32_t)(((uint64_t)u * m + t) >> 32);    // < 2m
+    const uint32_t z = redc_word(u, m, (uint32_t)t, (uint32_t)(t >> 32));   // < 2m
     const uint32_t r = min(z, z - m);                               // < m < 2^31
     const uint32_t x = r << b;                                      // < 2m
     return min(x, x - m);
@@ -285,21 +315,31 @@ __device__ __forceinline__ void w2_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0, 
         : "=r"(t1), "=r"(t2), "=r"(t3)
         : "r"((uint32_t)(a >> 32)), "r"((uint32_t)p), "r"((uint32_t)(p >> 32)), "r"((uint32_t)s),
           "r"((uint32_t)(s >> 32)));
-    // word step 1: (T + u0 m) / 2^32 = t1 + t2 2^32 + t3 2^64 + h0 + u0 m1
+    // word step 1: s = (T + u0 m) / 2^32 = (t1, t2, t3) + hi(u0 m0) + c + u0 m1,
+    // c the carry out of u0 m0 + t0 (whose low word is 0)
     const uint32_t u0 = t0 * mp;
-    const uint32_t h0 = (uint32_t)(((uint64_t)u0 * m0 + t0) >> 32);
-    const uint64_t g = (uint64_t)u0 * m1 + h0;
     uint32_t s0, s1, s2;
-    asm("add.cc.u32 %0, %3, %4;\n\t"
-        "addc.cc.u32 %1, %5, %6;\n\t"
-        "addc.u32 %2, %7, 0;"
+    asm("{\n\t.reg .u32 x, h, e2, e3;\n\t"
+        "mad.lo.cc.u32 x, %3, %4, %5;\n\t"
+        "madc.hi.cc.u32 h, %3, %4, %6;\n\t"
+        "addc.cc.u32 e2, %7, 0;\n\t"
+        "addc.u32 e3, %8, 0;\n\t"
+        "mad.lo.cc.u32 %0, %3, %9, h;\n\t"
+        "madc.hi.cc.u32 %1, %3, %9, e2;\n\t"
+        "addc.u32 %2, e3, 0;\n\t}"
         : "=r"(s0), "=r"(s1), "=r"(s2)
-        : "r"(t1), "r"((uint32_t)g), "r"(t2), "r"((uint32_t)(g >> 32)), "r"(t3));
-    // word step 2
+        : "r"(u0), "r"(m0), "r"(t0), "r"(t1), "r"(t2), "r"(t3), "r"(m1));
+    // word step 2: z = (s + u1 m) / 2^32 < 2m
     const uint32_t u1 = s0 * mp;
-    const uint32_t h1 = (uint32_t)(((uint64_t)u1 * m0 + s0) >> 32);
-    const uint64_t z = (((uint64_t)s2 << 32) | s1) + ((uint64_t)u1 * m1 + h1);   // < 2m
-    const uint32_t z0 = (uint32_t)z, z1 = (uint32_t)(z >> 32);
+    uint32_t z0, z1;
+    asm("{\n\t.reg .u32 x, h, e2;\n\t"
+        "mad.lo.cc.u32 x, %2, %3, %4;\n\t"
+        "madc.hi.cc.u32 h, %2, %3, %5;\n\t"
+        "addc.u32 e2, %6, 0;\n\t"
+        "mad.lo.cc.u32 %0, %2, %7, h;\n\t"
+        "madc.hi.u32 %1, %2, %7, e2;\n\t}"
+        : "=r"(z0), "=r"(z1)
+        : "r"(u1), "r"(m0), "r"(s0), "r"(s1), "r"(s2), "r"(m1));
     y1 = __funnelshift_l(z0, z1, b);
     y0 = z0 << b;
 }
@@ -323,36 +363,41 @@ __device__ __forceinline__ uint64_t w2_pow2(uint64_t E, uint64_t m, uint32_t mp)
 
 // --------------------------------------------------- width 2, m < 2^40 --
 // 2^32 <= m < 2^40 (m1 < 2^8), y in [0,4m) (y1 < 2^10). Same REDC_2^64 as
-// w2_sqr, arranged so that every multiply-add takes a full product as its
-// 64-bit addend: u0 m0 + y0^2 and u1 m0 + s wrap past 2^64 at most once and the
-// lost carry is recovered by an unsigned compare of the high words.
+// w2_sqr over the short top words: y^2 = y0^2 + y0 (2 y1) 2^32 + y1^2 2^64
+// with y0 (2 y1) < 2^43 and y1^2 < 2^20, so word step 1 is
+//   s = (y0^2 + u0 m0) / 2^32 + y1^2 2^32 + y0 (2 y1) + u0 m1 < 2^54,
+// one carry chain whose carry out of the first multiply-add lands on y1^2;
+// word step 2 is z = (s + u1 m0) / 2^32 + u1 m1 < 2m with its carry out
+// placed in the high word.
 __device__ __forceinline__ void w2s_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0, uint32_t m1, uint32_t mp,
                                         uint32_t b)
 {
     const uint64_t A = (uint64_t)y0 * y0;
-    const uint64_t P = (uint64_t)y0 * (y1 << 1);               // 2 y0 y1 < 2^43
     const uint32_t a0 = (uint32_t)A, a1 = (uint32_t)(A >> 32);
     const uint32_t u0 = a0 * mp;
-    const uint64_t X = (uint64_t)u0 * m0 + A;                 // low word 0; = (a1 + h0) 2^32 mod 2^64
-    const uint32_t x1 = (uint32_t)(X >> 32);
-    const uint32_t w = y1 * y1 + (x1 < a1 ? 1u : 0u);          // y1^2 < 2^20 plus the wrapped carry
-    const uint64_t Q = (uint64_t)u0 * m1 + P;                 // < 2^44
-    uint32_t s0, s1;                                           // s = (T + u0 m) / 2^32 < 2^54
-    asm("add.cc.u32 %0, %2, %3;\n\t"
-        "addc.u32 %1, %4, %5;"
+    const uint32_t ysq = y1 * y1;
+    const uint32_t y2 = y1 << 1;
+    uint32_t s0, s1;
+    asm("{\n\t.reg .u32 x0, x1, w, t0, t1;\n\t"
+        "mad.lo.cc.u32 x0, %2, %3, %4;\n\t"     // u0 m0 + y0^2: low word 0
+        "madc.hi.cc.u32 x1, %2, %3, %5;\n\t"
+        "addc.u32 w, %6, 0;\n\t"                // y1^2 + carry
+        "mad.lo.cc.u32 t0, %7, %8, x1;\n\t"     // + y0 (2 y1)
+        "madc.hi.u32 t1, %7, %8, w;\n\t"
+        "mad.lo.cc.u32 %0, %2, %9, t0;\n\t"     // + u0 m1
+        "madc.hi.u32 %1, %2, %9, t1;\n\t}"
         : "=r"(s0), "=r"(s1)
-        : "r"((uint32_t)Q), "r"(x1), "r"((uint32_t)(Q >> 32)), "r"(w));
-    const uint64_t s = ((uint64_t)s1 << 32) | s0;
+        : "r"(u0), "r"(m0), "r"(a0), "r"(a1), "r"(ysq), "r"(y0), "r"(y2), "r"(m1));
     const uint32_t u1 = s0 * mp;
-    const uint64_t Y = (uint64_t)u1 * m0 + s;                 // low word 0; = (s1 + h1) 2^32 mod 2^64
-    const uint32_t yw = (uint32_t)(Y >> 32);
-    const uint32_t c2 = yw < s1 ? 1u : 0u;
-    const uint64_t Zq = (uint64_t)u1 * m1;                    // < 2^40
-    uint32_t z0, z1;                                           // z = (s + u1 m) / 2^32 < 2m
-    asm("add.cc.u32 %0, %2, %3;\n\t"
-        "addc.u32 %1, %4, %5;"
+    uint32_t z0, z1;
+    asm("{\n\t.reg .u32 x0, yw, c2;\n\t"
+        "mad.lo.cc.u32 x0, %2, %3, %4;\n\t"     // u1 m0 + s: low word 0
+        "madc.hi.cc.u32 yw, %2, %3, %5;\n\t"
+        "addc.u32 c2, 0, 0;\n\t"
+        "mad.lo.cc.u32 %0, %2, %6, yw;\n\t"     // + u1 m1
+        "madc.hi.u32 %1, %2, %6, c2;\n\t}"
         : "=r"(z0), "=r"(z1)
-        : "r"((uint32_t)Zq), "r"(yw), "r"((uint32_t)(Zq >> 32)), "r"(c2));
+        : "r"(u1), "r"(m0), "r"(s0), "r"(s1), "r"(m1));
     y1 = __funnelshift_l(z0, z1, b);
     y0 = z0 << b;
 }
@@ -451,10 +496,15 @@ __device__ __forceinline__ uint64_t w2_digits(uint64_t r, uint64_t m, uint32_t m
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         q[j] = r0 * mp;
-        const uint32_t h = (uint32_t)(((uint64_t)q[j] * m0 + r0) >> 32);
-        const uint64_t w = (uint64_t)q[j] * m1 + h + r1;   // < m
-        r0 = (uint32_t)w;
-        r1 = (uint32_t)(w >> 32);
+        // (r + q m) / 2^32 = hi(q m0 + r) + c 2^32 + q m1 < m, c the carry out
+        asm("{\n\t.reg .u32 x, h, c;\n\t"
+            "mad.lo.cc.u32 x, %2, %3, %4;\n\t"
+            "madc.hi.cc.u32 h, %2, %3, %5;\n\t"
+            "addc.u32 c, 0, 0;\n\t"
+            "mad.lo.cc.u32 %0, %2, %6, h;\n\t"
+            "madc.hi.u32 %1, %2, %6, c;\n\t}"
+            : "=r"(r0), "=r"(r1)
+            : "r"(q[j]), "r"(m0), "r"(r0), "r"(r1), "r"(m1));
     }
     return ((uint64_t)r1 << 32) | r0;
 }

@@ -507,24 +507,26 @@ namespace cbl {
 __global__ void __launch_bounds__(256) probe_imad_kernel(uint32_t *sink, int iters)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    uint64_t w[16];
-    uint32_t a[16];
+    uint32_t x[16], a[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
         a[j] = t * 2654435761u + 7919u * j;
-        w[j] = t ^ (0x9e3779b9u * (j + 1));
+        x[j] = (t ^ (0x9e3779b9u * (j + 1))) | 1u;
     }
     const uint32_t k1 = 0x7feb352du;
-    // 16 independent accumulator chains; the multiplicands do not depend on them,
-    // so the issue rate (not the latency) of mad.wide is measured
+    // 16 independent chains x = x k1 + a: each multiply needs the previous
+    // one's result, so none can be hoisted out of the loop, and 16 chains per
+    // thread hide the latency: the issue rate of mad.lo.u32 (one multiply half
+    // each) is measured. A full 32x32 product (two halves) issues at half this
+    // rate, so the rate of halves is the same for wide products.
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(w[j]) : "r"(a[j]), "r"(k1));
+        for (int j = 0; j < 16; ++j) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(x[j]) : "r"(k1), "r"(a[j]));
     }
-    uint32_t x = 0;
+    uint32_t r = 0;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) x ^= (uint32_t)w[j] ^ (uint32_t)(w[j] >> 32);
-    sink[t] = x;
+    for (int j = 0; j < 16; ++j) r ^= x[j];
+    sink[t] = r;
 }
 
 int probe_imad_grid(int sm_count)
@@ -538,7 +540,7 @@ cudaError_t launch_probe_imad(uint32_t *sink, int grid, int block, int iters, ui
 {
     (void)block;
     probe_imad_kernel<<<grid, 256, 0, st>>>(sink, iters);
-    if (ops) *ops = (uint64_t)grid * block * (uint64_t)iters * 16ull * 2ull;   // two halves per mad.wide
+    if (ops) *ops = (uint64_t)grid * block * (uint64_t)iters * 16ull;   // one half per mad.lo
     return cudaGetLastError();
 }
 

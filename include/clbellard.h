@@ -173,8 +173,9 @@ int cbl_kernel_ms(cbl_ctx *ctx, float *ms);
 int cbl_prepared_info(const cbl_ctx *ctx, uint64_t *terms, uint64_t *tiles, int *segments, int *grid);
 
 /* ---- diagnostics */
-/* Peak rate of 32-bit multiply halves on this GPU (mad.wide.u32 chains, two
- * halves per instruction): the denominator of the term kernels' roofline. */
+/* Peak rate of 32-bit multiply halves on this GPU (dependent mad.lo.u32
+ * chains, one half per instruction): the denominator of the term kernels'
+ * roofline. */
 int cbl_probe_imad(cbl_ctx *ctx, int iters, double *ops_per_s, double *ms);
 /* Individual signed 192-bit terms (the per-term check of the oracle):
  * out3n[3*i..] = term k[i] of series f at position d; k >= d gives tail terms. */
