@@ -832,14 +832,17 @@ int cbl_run_job(cbl_ctx *c, uint64_t needD, int s, uint64_t b, uint64_t batchsiz
 // ---- balanced work-mode planning
 // Relative cost of one ladder step per residue kind (instructions per step
 // measured with ncu on GB300: about 7, 10, 13, 25, 28, 30).
+// Relative cost of one ladder step per residue kind, from each kind's measured
+// term rate on its own k-range (GB300): W1 7, W1M 9, W1S 11, W2S 18, W2 21;
+// W2X adds one 64-bit min to the W2 step.
 static double step_cost(uint64_t m)
 {
     if (m < kW1Max) return 7.0;
-    if (m < kW1MMax) return 10.0;
-    if (m < kW1SMax) return 13.0;
-    if (m < kW2SMax) return 25.0;
-    if (m < kW2Max) return 28.0;
-    return 30.0;
+    if (m < kW1MMax) return 9.0;
+    if (m < kW1SMax) return 11.0;
+    if (m < kW2SMax) return 18.0;
+    if (m < kW2Max) return 21.0;
+    return 22.0;
 }
 
 // Estimated cost of terms k in [k0, k1) of series f at position d (k < d):
@@ -882,20 +885,13 @@ int cbl_plan_jobs(uint64_t needD, int njobs, int *out_s, uint64_t *out_k0, uint6
     if (rc) return rc;
     double cost[7], total = 0;
     for (int f = 0; f < 7; ++f) total += cost[f] = range_cost(d, f, 0, d) + 1.0;
-    // jobs per series in proportion to its cost, at least one each
-    int per[7], used = 0;
+    // jobs per series: one each, then each further job to the series whose cost
+    // per job is largest (this minimises the largest job for a fixed count)
     // (at most d jobs per series: each job keeps at least one term below d)
     const int maxper = (int)std::min<uint64_t>(d, (uint64_t)njobs);
-    for (int f = 0; f < 7; ++f) {
-        per[f] = std::min(maxper, std::max(1, (int)(njobs * cost[f] / total)));
-        used += per[f];
-    }
-    while (used > njobs) {
-        int f = (int)(std::max_element(per, per + 7) - per);
-        --per[f];
-        --used;
-    }
-    while (used < njobs) {                                  // give the rest to the heaviest cost per job
+    int per[7], used = 7;
+    for (int f = 0; f < 7; ++f) per[f] = 1;
+    while (used < njobs) {
         int best = -1;
         for (int f = 0; f < 7; ++f)
             if (per[f] < maxper && (best < 0 || cost[f] / per[f] > cost[best] / per[best])) best = f;

@@ -114,7 +114,7 @@ def test_plan_balances_modelled_cost(cbl, oracle):
         k = np.arange(k0, min(k1, d), dtype=np.uint64)
         bits = np.floor(np.log2((10 * (d - k)).astype(np.float64))) + 1
         m = den[s][0] * k + den[s][1]
-        step = np.where(m < 2 ** 28, 7.0, 10.0)            # m < 4e6 here: the two smallest kinds
+        step = np.where(m < 2 ** 28, 7.0, 9.0)             # m < 4e6 here: the two smallest kinds
         costs.append(float(((bits + 8) * step).sum()))
     assert max(costs) / min(costs) < 1.10
 
