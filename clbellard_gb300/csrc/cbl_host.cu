@@ -14,6 +14,7 @@
 #include <thread>
 #include <vector>
 #include <sys/stat.h>
+#include <unistd.h>
 #include <sys/types.h>
 
 using namespace cbl;
@@ -979,13 +980,24 @@ int cbl_job_write(const char *workdir, int s, uint64_t b, const char *hex, int d
     std::snprintf(dir, sizeof dir, "/%d", s);
     if (mkdir_p(std::string(workdir) + dir) != 0) return CBL_E_IO;
     const std::string p = job_path(workdir, s, b);
-    FILE *f = std::fopen(p.c_str(), "wb");
+    // Written to a temporary name in the same directory and renamed into place,
+    // so a process killed mid-write leaves no partial job file: the job then
+    // simply counts as not done. (The reference writes the file in place,
+    // Bellard_192.hsp:514-533.)
+    char suffix[48];
+    std::snprintf(suffix, sizeof suffix, ".tmp%ld", (long)getpid());
+    const std::string tmp = p + suffix;
+    FILE *f = std::fopen(tmp.c_str(), "wb");
     if (!f) return CBL_E_IO;
     // HSP writes "\n" as CR LF; the layout is hex / device no TAB name / ms "ms"
     const int w = std::fprintf(f, "%.48s\r\n%d\t%s\r\n%lldms", hex, deviceno, devname ? devname : "",
                                (long long)ms);
     const int cl = std::fclose(f);
-    return (w < 0 || cl != 0) ? CBL_E_IO : CBL_OK;
+    if (w < 0 || cl != 0 || std::rename(tmp.c_str(), p.c_str()) != 0) {
+        std::remove(tmp.c_str());
+        return CBL_E_IO;
+    }
+    return CBL_OK;
 }
 
 int cbl_job_read(const char *workdir, int s, uint64_t b, char hex[49])

@@ -1,27 +1,13 @@
 """Work-mode host logic on the CPU: worklist format, job files, the
-workmodeSum merge, and sharding jobs over 2 gloo ranks. Job partials come from
-the oracle here (the CPU stands in for the GPUs only in this test)."""
+workmodeSum merge, balanced plans, and sharding jobs over 2 gloo ranks. Job
+partials come from the oracle here (the CPU stands in for the GPUs only in
+these tests)."""
 import os
 
 import pytest
 
 from conftest import load_golden
-
-
-def oracle_job(oracle, batchsize):
-    """The reference's job partial (numer-weighted, 192-bit) from the oracle."""
-    def fn(needD, s, b, bs):
-        d, _ = oracle.pos_to_d(needD)
-        k0, k1 = b * bs, (b + 1) * bs
-        if k0 > d:
-            return None
-        kend = min(k1, d)
-        v = oracle.sum_range(d, s, k0, kend, 3) if k0 < kend else 0
-        if max(k0, kend) == d:                        # tail when the range reaches d
-            v += oracle.sum_range(d, s, d, d + 20, 3)
-        v = (v << oracle.NUMER_LOG2[s]) % (1 << 192)
-        return "%048x" % v
-    return fn
+from workmode_helpers import oracle_job, oracle_range
 
 
 def test_parse_sample_worklist():
@@ -69,20 +55,6 @@ def test_skip_past_d(cbl, oracle):
     fn = oracle_job(oracle, 1000)
     d, _ = oracle.pos_to_d(10000)
     assert fn(10000, 0, d // 1000 + 1, 1000) is None
-
-
-def oracle_range(oracle):
-    """Job partial over an explicit k-range (the tail when the range reaches d)."""
-    def fn(needD, s, k0, k1):
-        d, _ = oracle.pos_to_d(needD)
-        if k0 > d:
-            return None
-        kend = min(k1, d)
-        v = oracle.sum_range(d, s, k0, kend, 3) if k0 < kend else 0
-        if max(k0, kend) == d:
-            v += oracle.sum_range(d, s, d, d + 20, 3)
-        return "%048x" % ((v << oracle.NUMER_LOG2[s]) % (1 << 192))
-    return fn
 
 
 @pytest.mark.parametrize("needD,njobs", [(10, 7), (10, 50), (100000, 16), (10 ** 10, 64), (10 ** 17, 200)])
@@ -151,6 +123,7 @@ def _rank_main(rank, world, port, needD, bs, out_q):
     try:
         from oracle import oracle
         from clbellard_gb300 import workmode as W
+        from workmode_helpers import oracle_job
         d, _ = oracle.pos_to_d(needD)
         fn = oracle_job(oracle, bs)
         mine = [fn(needD, s, b, bs) for s, b in W.shard(W.all_jobs(d, bs), rank, world)]
