@@ -21,7 +21,7 @@ def test_dd_digits_kept(ctxdd, p):
 
 
 def test_dd_1e8_vs_reference_mode0(ctxdd):
-    s = load_golden("survey_probe.json")
+    s = load_golden("recorded_probe.json")
     h = ctxdd.compute(10 ** 8)
     assert agree(h, s["exact256"]["100000000"]) >= 19
     assert agree(h, s["ref_mode0_prefix"]["100000000"]) >= 19

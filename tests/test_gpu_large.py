@@ -36,7 +36,7 @@ def test_1e9(ctx192):
     pub = load_golden("published_digits.json")["digits"]
     h = ctx192.compute(10 ** 9)
     assert h.startswith(pub["1000000000"])
-    s = load_golden("survey_probe.json")
+    s = load_golden("recorded_probe.json")
     assert agree(h, s["exact256"]["1000000000"]) >= 33
 
 

@@ -29,7 +29,7 @@ def test_precision_2_equals_1(ctx_beta):
 
 
 def test_1e8_against_oracle(ctx192):
-    s = load_golden("survey_probe.json")
+    s = load_golden("recorded_probe.json")
     pub = load_golden("published_digits.json")["digits"]
     h = ctx192.compute(10 ** 8)
     assert h.startswith(pub["100000000"])

@@ -78,9 +78,9 @@ def test_known_pi_prefix(oracle):
     assert oracle.to_hex(oracle.result(d, 0, 4), 4).startswith("6a8885a308d313198a2e0370734")
 
 
-def test_exact_oracle_against_survey_and_published():
+def test_exact_oracle_against_recorded_and_published():
     g = load_golden("oracle_small.json")
-    s = load_golden("survey_probe.json")
+    s = load_golden("recorded_probe.json")
     pub = load_golden("published_digits.json")["digits"]
     from oracle.oracle import agreeing_hex_digits as agree
     for p in ("1000000", "10000000"):
@@ -100,7 +100,7 @@ def test_big_fixture_consistency():
     if not os.path.exists(path):
         pytest.skip("oracle_big.json not generated")
     g = load_golden("oracle_big.json")
-    s = load_golden("survey_probe.json")
+    s = load_golden("recorded_probe.json")
     pub = load_golden("published_digits.json")["digits"]
     for p, v in g.items():
         assert v["hex256"].startswith(pub[p])
@@ -152,10 +152,10 @@ def test_oracle_against_reference_kernels(oracle):
         assert e["mode0"].endswith("0" * 20)
 
 
-def test_reference_outputs_match_survey_record():
-    """The harness reproduces the reference outputs recorded in the survey."""
+def test_reference_outputs_match_recorded_probe():
+    """The harness reproduces the recorded reference outputs (an independent earlier run)."""
     ref = load_golden("ref_outputs.json")
-    s = load_golden("survey_probe.json")
+    s = load_golden("recorded_probe.json")
     for p, h in s["ref_mode2"].items():
         if p in ref:
             assert ref[p]["mode2"] == h
