@@ -242,7 +242,7 @@ int run_segments(cbl_ctx *c, std::vector<Seg> &v)
 
 int dd_range(cbl_ctx *c, uint64_t k0, uint64_t k1, uint64_t d, int sign, uint32_t den0, uint32_t den1)
 {
-    if (k1 > k0 && (u128)den0 * (k1 - 1) + den1 >= (u128)kDDMax) return CBL_E_POSITION;
+    if (k1 > k0 && (u128)den0 * (k1 - 1) + den1 >= (u128)kW2XMax) return CBL_E_POSITION;
     // chunks of 2^30 terms keep each launch to a bounded time
     const uint64_t chunk = 1ull << 30;
     for (uint64_t a = k0; a < k1; a += chunk) {
@@ -334,7 +334,7 @@ const char *cbl_strerror(int code)
     case CBL_SKIPPED: return "job skipped: k_start > d";
     case CBL_E_ARG: return "invalid argument";
     case CBL_E_POSITION:
-        return "invalid position (outside [5, 999999999999999999], or a modulus >= 2^53 in mode 0)";
+        return "invalid position (outside [5, 999999999999999999])";
     case CBL_E_NODEVICE: return "no CUDA device";
     case CBL_E_CUDA: return "CUDA runtime error";
     case CBL_E_TIMEOUT: return "timed out waiting for the device";
@@ -582,7 +582,7 @@ int cbl_BatchCalc(cbl_ctx *c, uint64_t k_start, uint64_t k_end, int f, uint64_t 
             if (rc) return rc;
         }
         if (tail) {
-            if ((u128)kDen0[f] * (d + kTailDD) + kDen1[f] >= (u128)kDDMax) return CBL_E_POSITION;
+            if ((u128)kDen0[f] * (d + kTailDD) + kDen1[f] >= (u128)kW2XMax) return CBL_E_POSITION;
             CK(launch_dd_tail(c->d_bigsum, d, kSign[f], kDen0[f], kDen1[f], c->st));
             c->launches++;
         }

@@ -20,7 +20,7 @@ constexpr uint64_t kW1SMax = 1ull << 32;  // strict width 1 for 2^31 <= m < 2^32
 constexpr uint64_t kW2SMax = 1ull << 40;  // short width 2 for 2^32 <= m < 2^40
 constexpr uint64_t kW2Max = 1ull << 60;   // width 2 (two words, residues < 4m) for m < 2^60
 constexpr uint64_t kW2XMax = 1ull << 62;  // wide width 2 (residues < 2m) for 2^60 <= m < 2^62
-constexpr uint64_t kDDMax = 1ull << 53;   // double-double mode: m and r exact as doubles
+constexpr uint64_t kDDMax = 1ull << 53;   // double-double mode: m and r exact as doubles below, double-doubles above
 
 constexpr int kTail192 = 20;   // tail terms k = d..d+19 (Bellard.cl:1164-1239)
 constexpr int kTailDD = 10;    // tail terms k = d..d+9  (Bellard.cl:1125)

@@ -371,6 +371,32 @@ __device__ __forceinline__ DD dd_div_nn(double x, double y)
     return two_sum(q1, q2);
 }
 
+// An integer 0 <= x < 2^63 as an exact double-double: hi = x rounded to 53
+// bits, lo = the (small, signed) rest.
+__device__ __forceinline__ DD dd_from_u64(uint64_t x)
+{
+    const double hi = __ull2double_rn(x);
+    const int64_t rest = (int64_t)(x - __double2ull_rn(hi));
+    return DD{hi, (double)rest};
+}
+
+// a / b for exact double-doubles a >= 0, b > 0 of integers (the OVERDOUBLE case
+// m >= 2^53 of Bellard.cl:937-945, 1040-1047): q1 = a.hi / b.hi, the remainder
+// a - q1 b formed with an exact product (fma) and a single rounding of the
+// q1 b.lo term, then one correction quotient. For b ~ 2^e the remainder is
+// ~2^(e-53) and carries errors ~2^(e-106), so the quotient keeps ~104 bits.
+__device__ __forceinline__ DD dd_div_dd(DD a, DD b)
+{
+    const double q1 = a.hi / b.hi;
+    const double p_hi = q1 * b.hi;
+    const double p_lo = fma(q1, b.hi, -p_hi);            // q1 b.hi = p_hi + p_lo exactly
+    double e = a.hi - p_hi;                               // exact: p_hi is within a factor 2 of a.hi
+    e += a.lo - p_lo;
+    e = fma(-q1, b.lo, e);
+    const double q2 = e / b.hi;
+    return two_sum(q1, q2);
+}
+
 constexpr int kBlockDD = 256;
 
 __device__ __forceinline__ DD block_reduce_dd(DD v)
@@ -407,8 +433,10 @@ __global__ void __launch_bounds__(kBlockDD) dd_terms_kernel(double2 *bigsum, uin
         else if (m < kW1MMax) r = w1_digits(w1m_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
         else if (m < kW1SMax) r = w1_digits(w1s_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
         else if (m < kW2SMax) r = w2_digits(w2s_pow2(E, m, mp), m, mp, q);
-        else r = w2_digits(w2_pow2(E, m, mp), m, mp, q);
-        DD t = dd_div_nn((double)r, (double)m);
+        else if (m < kW2Max) r = w2_digits(w2_pow2(E, m, mp), m, mp, q);
+        else r = w2_digits(w2x_pow2(E, m, mp), m, mp, q);
+        // r and m are exact doubles below 2^53; above, exact double-doubles
+        DD t = (m < kDDMax) ? dd_div_nn((double)r, (double)m) : dd_div_dd(dd_from_u64(r), dd_from_u64(m));
         if ((k + (uint64_t)sign) & 1ull) { t.hi = -t.hi; t.lo = -t.lo; }
         sum = dd_frac(dd_add(sum, t));
     }
@@ -436,7 +464,7 @@ __global__ void dd_tail_kernel(double2 *bigsum, uint64_t d, int sign, uint32_t d
         const uint64_t k = d + (uint64_t)i;
         const uint64_t m = (uint64_t)den0 * k + den1;
         if (m != 1) {
-            DD t = dd_div_nn(p, (double)m);
+            DD t = (m < kDDMax) ? dd_div_nn(p, (double)m) : dd_div_dd(DD{p, 0.0}, dd_from_u64(m));
             if ((k + (uint64_t)sign) & 1ull) { t.hi = -t.hi; t.lo = -t.lo; }
             sum = dd_add(sum, t);
         }

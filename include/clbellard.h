@@ -39,8 +39,7 @@ extern "C" {
 #define CBL_OK            0
 #define CBL_SKIPPED       1   /* job not run: k_start > d (Bellard_192.hsp:306) */
 #define CBL_E_ARG        -1   /* bad argument (null pointer, bad formula index) */
-#define CBL_E_POSITION   -2   /* position outside [5, 999999999999999999] (Bellard_192.hsp:449-450), or a
-                                 modulus >= 2^53 in mode 0 (positions above ~2.25e15) */
+#define CBL_E_POSITION   -2   /* position outside [5, 999999999999999999] (Bellard_192.hsp:449-450) */
 #define CBL_E_NODEVICE   -3   /* no CUDA device / bad device index */
 #define CBL_E_CUDA       -4   /* a CUDA runtime call failed */
 #define CBL_E_TIMEOUT    -5   /* cbl_wait gave up */
@@ -73,8 +72,9 @@ int cbl_Set0ans(cbl_ctx *ctx);
 int cbl_Sglobal32mtg(cbl_ctx *ctx, uint64_t offset, uint64_t d, uint64_t k_max,
                      int64_t numesign, uint64_t den0, uint64_t den1);
 /* Sglobal64mtg / Sglobal64mtg_192 / Sglobal64mtg_192_Refresh (Bellard.cl:914-1092,
- * Bellard_div2by1.cl:313-359): same contract for any modulus below 2^62
- * (below 2^53 in mode 0). */
+ * Bellard_div2by1.cl:313-359): same contract for any modulus below 2^62. In
+ * mode 0, moduli from 2^53 up take the OVERDOUBLE route (Bellard.cl:937-945):
+ * r and m as exact double-doubles and a double-double division. */
 int cbl_Sglobal64mtg(cbl_ctx *ctx, uint64_t offset, uint64_t d, uint64_t k_max,
                      int64_t numesign, uint64_t den0, uint64_t den1);
 /* Sglobal_after / Sglobal_after_192 (Bellard.cl:1118-1253): the tail terms

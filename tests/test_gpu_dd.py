@@ -43,3 +43,39 @@ def test_dd_flow_and_jobs(ctxdd, oracle):
     assert len(h) == 48
     with pytest.raises(Exception):
         ctxdd.batch([1000])
+
+
+def _dd_mod1(hi, lo):
+    from fractions import Fraction
+    return (Fraction(hi) + Fraction(lo)) % 1
+
+
+def _close_mod1(x, y, tol):
+    t = (x - y) % 1
+    return min(t, 1 - t) < tol
+
+
+@pytest.mark.parametrize("needD", [10 ** 16, 999999999999999995])
+def test_dd_overdouble_against_exact(ctxdd, oracle, needD):
+    """Moduli >= 2^53 in mode 0 (the reference's OVERDOUBLE build): r and m
+    as exact double-doubles, divided in double-double. Sampled ranges just
+    across 2^53, just below d (up to 2^62 near the position limit) and the
+    10-term tail agree with the exact 256-bit oracle to 2^-90."""
+    from fractions import Fraction
+    d, _ = oracle.pos_to_d(needD)
+    tol = Fraction(1, 2 ** 90)
+    for f in range(7):
+        den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
+        k53 = ((1 << 53) - den1 + den0 - 1) // den0
+        for k0, k1 in [(k53 - 2048, k53 + 2048), (d - 4096, d - 1)]:     # k1 < d: no tail here
+            ctxdd.Set0mem()
+            ctxdd.BatchCalc(k0, k1, f, d)
+            got = _dd_mod1(*ctxdd.read_partial())
+            want = Fraction(oracle.sum_range(d, f, k0, k1, 4), 2 ** 256)
+            assert _close_mod1(got, want, tol), (f, k0, float((got - want) % 1))
+        ctxdd.Set0mem()
+        ctxdd.Sglobal_after(d, oracle.SIGN[f], den0, den1)
+        ctxdd.Ssum()
+        got = _dd_mod1(*ctxdd.read_partial())
+        want = Fraction(oracle.sum_range(d, f, d, d + 10, 4), 2 ** 256)
+        assert _close_mod1(got, want, tol), (f, "tail")
