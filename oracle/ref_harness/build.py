@@ -1,5 +1,7 @@
 """Compile the reference's own kernels (Bellard.cl, Bellard_div2by1.cl) as
-C++ for the CPU into oracle/_ref/ref_bellard.
+C++ for the CPU into oracle/_ref/ref_bellard, and a second time with
+-DOVERDOUBLE into oracle/_ref/ref_bellard_od (the build the reference's host
+selects when a modulus can reach 2^53, Bellard_192.hsp:472).
 
 TEST INFRASTRUCTURE: the reference run here pins the oracle and gives a CPU
 baseline. The sources are read from the reference tree where they lie; a
@@ -21,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
 BINARY = os.path.join(OUT_DIR, "ref_bellard")
+BINARY_OD = os.path.join(OUT_DIR, "ref_bellard_od")
 REFERENCE = "/root/reference"
 SOURCES = ("Bellard.cl", "Bellard_div2by1.cl")
 LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
@@ -36,7 +39,8 @@ def build_if_available(force: bool = False):
     if not available():
         return BINARY if os.path.exists(BINARY) else None
     deps = [os.path.join(HERE, "harness.cpp"), os.path.join(HERE, "shim.h"), __file__]
-    if not force and os.path.exists(BINARY) and all(os.path.getmtime(p) < os.path.getmtime(BINARY) for p in deps):
+    if not force and all(os.path.exists(b) and all(os.path.getmtime(p) < os.path.getmtime(b) for p in deps)
+                         for b in (BINARY, BINARY_OD)):
         return BINARY
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = tempfile.mkdtemp(prefix="cbl_ref_")
@@ -44,12 +48,13 @@ def build_if_available(force: bool = False):
         for s in SOURCES:
             text = open(os.path.join(REFERENCE, s), encoding="utf-8").read()
             open(os.path.join(tmp, s), "w", encoding="utf-8").write(LOCAL_ARRAY.sub(r"\1static thread_local\2", text))
-        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-w",
-               "-I", tmp, "-I", HERE, os.path.join(HERE, "harness.cpp"), "-o", BINARY + ".tmp"]
-        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("reference harness build failed:\n" + r.stdout[-4000:])
-        os.replace(BINARY + ".tmp", BINARY)
+        for out, extra in ((BINARY, []), (BINARY_OD, ["-DOVERDOUBLE"])):
+            cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-w", *extra,
+                   "-I", tmp, "-I", HERE, os.path.join(HERE, "harness.cpp"), "-o", out + ".tmp"]
+            r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("reference harness build failed:\n" + r.stdout[-4000:])
+            os.replace(out + ".tmp", out)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     return BINARY
@@ -95,6 +100,34 @@ def run(needD: int, precision: int, groups: int = 64, threads: int = 0, timeout:
             res["terms_per_s"] = float(v)
         elif k == "threads":
             res["threads"] = int(v)
+    return res
+
+
+def run_range(needD: int, precision: int, f: int, k0: int, k1: int, groups: int = 64, threads: int = 0,
+              timeout: float = 600.0) -> dict:
+    """The reference's BatchCalc for series f over k in [k0, min(k1, d)) (plus
+    the tail when the range reaches d), after Ssum and before Sum7: returns d
+    and the partial as an int (modes 1-2, bigSum[0..2]) or (hi, lo) (mode 0).
+    Uses the OVERDOUBLE build when the reference's host would
+    (d*10+9 >= 2^53, Bellard_192.hsp:472)."""
+    if build_if_available() is None:
+        raise RuntimeError("reference harness not built and the reference tree is absent")
+    d = ((needD - 1) * 2 - 3) // 5
+    if d % 2 == 0:
+        d -= 1
+    b = BINARY_OD if d * 10 + 9 >= (1 << 53) else BINARY
+    args = [b, "range", str(needD), str(precision), str(f), str(k0), str(k1), str(groups), str(threads)]
+    out = subprocess.run(args, stdout=subprocess.PIPE, text=True, timeout=timeout, check=True).stdout
+    res = {"overdouble": b == BINARY_OD}
+    for ln in out.splitlines():
+        k, _, v = ln.partition(" ")
+        if k == "d":
+            res["d"] = int(v)
+        elif k == "partial":
+            res["partial"] = int(v, 16)
+        elif k == "partial_dd":
+            hi, lo = v.split()
+            res["partial"] = (float(hi), float(lo))
     return res
 
 

@@ -12,6 +12,11 @@
  * With k0 k1 chunks: a timing sample instead of a full position: for every
  * series, `chunks` ranges of (k1-k0) terms spread evenly over [0, d) run as the
  * reference's BatchCalc main loops (no tail); terms/s counts those terms.
+ *
+ *   ref_bellard range <needD> <precision> <f> <k0> <k1> [groups=64] [threads=all]
+ *   prints: d, and the series-f partial over k in [k0, min(k1, d)) plus the
+ *   tail when the range reaches d, after Ssum and before Sum7 (the reference's
+ *   BatchCalc for one series: bigSum[0..2] as 48 hex, or the dd pair).
  */
 #include "shim.h"
 
@@ -110,15 +115,31 @@ static void launch(ulong global, int local, const std::function<void()> &body, i
 
 int main(int argc, char **argv)
 {
+    const bool range = argc > 1 && !strcmp(argv[1], "range");
+    if (range) {
+        if (argc < 7) {
+            fprintf(stderr, "usage: ref_bellard range needD precision f k0 k1 [groups] [threads]\n");
+            return 2;
+        }
+        ++argv;                                          // the rest reads like the position form
+        --argc;
+    }
     if (argc < 3) {
         fprintf(stderr, "usage: ref_bellard needD precision [groups] [threads]\n");
         return 2;
     }
     long long needD = atoll(argv[1]);
     const int precision = atoi(argv[2]);
+    const int rf = range ? atoi(argv[3]) : -1;
+    const ulong rk0 = range ? strtoull(argv[4], nullptr, 10) : 0, rk1 = range ? strtoull(argv[5], nullptr, 10) : 0;
+    if (range) {                                         // groups / threads follow the range arguments
+        argv += 3;
+        argc -= 3;
+        if (rf < 0 || rf > 6 || rk1 < rk0) return 2;
+    }
     const int groups = argc > 3 ? atoi(argv[3]) : 64;
     const int threads = argc > 4 && atoi(argv[4]) > 0 ? atoi(argv[4]) : omp_get_max_threads();
-    const bool sample = argc > 7;
+    const bool sample = !range && argc > 7;
     const long long slen = sample ? atoll(argv[6]) - atoll(argv[5]) : 0;
     const int nchunks = sample ? atoi(argv[7]) : 1;
     if (needD <= 4) return 2;
@@ -137,16 +158,22 @@ int main(int argc, char **argv)
     auto t0 = std::chrono::steady_clock::now();
     long long sample_terms = 0;
     for (int fc = 0; fc < 7 * nchunks; ++fc) {
-        const int f = fc / nchunks;
+        const int f = range ? rf : fc / nchunks;
+        if (range && fc > 0) break;
         std::fill(bigSum.begin(), bigSum.end(), 0);              // Set0memUlong3 / Set0memdd
         // BatchCalc k_start, k_end, f (KernelFuncs.as:25-66); the whole of [0, d) unless sampling
         ulong k_start = 0, k_end = (ulong)d;
+        if (range) {
+            k_start = std::min(rk0, (ulong)d);
+            k_end = std::min(rk1, (ulong)d);
+        }
         if (sample) {
             k_start = (ulong)((long double)d * (fc % nchunks) / nchunks);
             k_end = std::min((ulong)d, k_start + (ulong)slen);
             sample_terms += (long long)(k_end - k_start);
         }
         ulong k_max = k_start, offset = k_start;
+        if (range && rk0 > (ulong)d) offset = rk0;               // past d: nothing runs (Bellard_192.hsp:306)
         ulong loopmax32 = (((ulong)1 << 32) - den1[f] - 1) / den0[f] + 1;
         if (loopmax32 > (ulong)d) loopmax32 = d;
         if (loopmax32 > k_end) loopmax32 = k_end;
@@ -171,7 +198,7 @@ int main(int argc, char **argv)
             offset = k_max;
         }
         if (sample) continue;
-        if (offset == (ulong)d) {
+        if (offset == (ulong)d) {                                // KernelFuncs.as: the tail when the loops reach d
             if (precision == 0)
                 launch(1, 1, [&] { bellard::Sglobal_after((double2 *)bigD, d, nsign[f], den0[f], den1[f]); }, 1);
             else
@@ -183,14 +210,25 @@ int main(int argc, char **argv)
             launch(256, kLocal, [&] { bellard::Ssum((const double2 *)bigD, (double2 *)smallSum.data()); }, 1);
             bigD[0] = ((double *)smallSum.data())[0];
             bigD[1] = ((double *)smallSum.data())[1];
+            if (range) break;
             launch(1, 1, [&] { bellard::Sum7((double2 *)ansD, (double2 *)bigD, numer[f]); }, 1);
         } else {
             launch(256, kLocal, [&] { bellard::Ssum_192(bigSum.data(), smallSum.data()); }, 1);
             bigSum[0] = smallSum[0];
             bigSum[1] = smallSum[1];
             bigSum[2] = smallSum[2];
+            if (range) break;
             launch(1, 1, [&] { bellard::Sum7_192(dev_ans.data(), bigSum.data(), numer[f]); }, 1);
         }
+    }
+    if (range) {
+        printf("d %lld\n", d);
+        if (precision == 0)
+            printf("partial_dd %.17g %.17g\n", bigD[0], bigD[1]);
+        else
+            printf("partial %016llx%016llx%016llx\n", (unsigned long long)bigSum[0], (unsigned long long)bigSum[1],
+                   (unsigned long long)bigSum[2]);
+        return 0;
     }
     const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     printf("d %lld\n", d);

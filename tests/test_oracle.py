@@ -162,3 +162,47 @@ def test_reference_outputs_match_recorded_probe():
     for p, h in s["ref_mode0_prefix"].items():
         if p in ref:
             assert ref[p]["mode0"].startswith(h)
+
+
+def _ref_range_exact(oracle, r):
+    """The oracle's 192-bit partial for one reference range record."""
+    d, f, k0, k1 = r["d"], r["f"], r["k0"], r["k1"]
+    kend = min(k1, d)
+    v = oracle.sum_range(d, f, k0, kend, 3) if k0 < kend else 0
+    if max(k0, kend) == d:
+        v += oracle.sum_range(d, f, d, d + 20, 3)
+    return v % (1 << 192)
+
+
+def _ulp_dist(a, b, bits=192):
+    t = (a - b) % (1 << bits)
+    return min(t, (1 << bits) - t)
+
+
+def test_oracle_against_reference_64bit_kernels():
+    """Per-series partials of the reference's own kernels over short k-ranges
+    at positions 1e10 ... 999999999999999995 (moduli up to 2^62, the
+    OVERDOUBLE build above 2^53): on ranges with every modulus >= 2^32 the
+    reference's exact integer kernel (Sglobal64mtg_192_Refresh, mode 2)
+    equals the oracle bit for bit; where its dd-based 32-bit kernel or tail
+    takes part, and in mode 1, it is within 64 units of 2^-192; mode 0 (dd)
+    is within 2^-96."""
+    from fractions import Fraction
+    from oracle import oracle
+    oracle.build()
+    recs = load_golden("ref_ranges.json")["records"]
+    assert len(recs) >= 150 and any(r["overdouble"] for r in recs)
+    n_exact = 0
+    for r in recs:
+        v = _ref_range_exact(oracle, r)
+        m2, m1 = int(r["mode2"], 16), int(r["mode1"], 16)
+        if r["exact"]:
+            assert m2 == v, r
+            n_exact += 1
+        else:
+            assert _ulp_dist(m2, v) <= 64, r
+        assert _ulp_dist(m1, v) <= 64, r
+        hi, lo = r["mode0"]
+        t = ((Fraction(hi) + Fraction(lo)) - Fraction(v, 1 << 192)) % 1
+        assert min(t, 1 - t) < Fraction(1, 2 ** 96), r
+    assert n_exact >= 70
