@@ -16,6 +16,17 @@
 #include <sys/stat.h>
 #include <unistd.h>
 #include <sys/types.h>
+#include <new>
+
+// Every int-returning entry point runs inside this guard, so no C++ exception
+// crosses the C ABI: a failed host allocation returns CBL_E_NOMEM, anything
+// else CBL_E_ARG.
+#define CBL_GUARD_BEGIN try {
+#define CBL_GUARD_END                                                                   \
+    }                                                                                   \
+    catch (const std::bad_alloc &) { return CBL_E_NOMEM; }                              \
+    catch (...) { return CBL_E_ARG; }
+
 
 using namespace cbl;
 
@@ -350,26 +361,31 @@ const char *cbl_strerror(int code)
 
 int cbl_formula(int f, uint64_t *numer, int64_t *numesign, uint64_t *den0, uint64_t *den1)
 {
+    CBL_GUARD_BEGIN
     if (!formula_ok(f)) return CBL_E_ARG;
     if (numer) *numer = (uint64_t)kNumer[f];
     if (numesign) *numesign = kSign[f];
     if (den0) *den0 = kDen0[f];
     if (den1) *den1 = kDen1[f];
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_pos_to_d(uint64_t needD, uint64_t *d, uint64_t *needD_adj)
 {
+    CBL_GUARD_BEGIN
     if (needD <= 4 || needD > kMaxNeedD) return CBL_E_POSITION;
     uint64_t dd = ((needD - 1) * 2 - 3) / 5;
     if (dd % 2 == 0) dd--;
     if (d) *d = dd;
     if (needD_adj) *needD_adj = (dd * 5 + 3) / 2 + 1;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_create(int device, int precision, cbl_ctx **out)
 {
+    CBL_GUARD_BEGIN
     if (!out || precision < 0 || precision > 2) return CBL_E_ARG;
     *out = nullptr;
     int n = 0;
@@ -412,10 +428,12 @@ int cbl_create(int device, int precision, cbl_ctx **out)
     }
     *out = c;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_destroy(cbl_ctx *c)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
@@ -439,6 +457,7 @@ int cbl_destroy(cbl_ctx *c)
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_precision(const cbl_ctx *c) { return c ? c->precision : CBL_E_ARG; }
@@ -447,13 +466,16 @@ int64_t cbl_launch_count(const cbl_ctx *c) { return c ? c->launches : CBL_E_ARG;
 
 int cbl_device_name(const cbl_ctx *c, char *buf, int len)
 {
+    CBL_GUARD_BEGIN
     if (!c || !buf || len <= 0) return CBL_E_ARG;
     std::snprintf(buf, (size_t)len, "%s", c->devname);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_set_tuning(cbl_ctx *c, int tile_terms, int ctas_per_sm)
 {
+    CBL_GUARD_BEGIN
     if (!c || tile_terms < 32 || tile_terms % 32 != 0 || ctas_per_sm < 0) return CBL_E_ARG;
     if (c->partial) return CBL_E_ARG;                 // a budgeted run depends on the tile numbering
     const bool renumber = tile_terms != c->tile_k && c->prep_npos > 0;
@@ -465,32 +487,39 @@ int cbl_set_tuning(cbl_ctx *c, int tile_terms, int ctas_per_sm)
         return upload_prepared(c);
     }
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_set_graph(cbl_ctx *c, int enable)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     c->use_graph = enable != 0;
     drop_graph(c);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_Set0mem(cbl_ctx *c)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     cudaSetDevice(c->device);
     if (is192(c)) CK(cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6, c->st));
     else CK(cudaMemsetAsync(c->d_bigsum, 0, sizeof(double2) * kDDBlocks, c->st));
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_Set0ans(cbl_ctx *c)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     cudaSetDevice(c->device);
     if (is192(c)) CK(cudaMemsetAsync(c->d_ans, 0, sizeof(uint64_t) * 3, c->st));
     else CK(cudaMemsetAsync(c->d_ddans, 0, sizeof(double2), c->st));
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 static int sglobal(cbl_ctx *c, uint64_t offset, uint64_t d, uint64_t k_max, int64_t numesign, uint64_t den0,
@@ -513,17 +542,22 @@ static int sglobal(cbl_ctx *c, uint64_t offset, uint64_t d, uint64_t k_max, int6
 int cbl_Sglobal32mtg(cbl_ctx *c, uint64_t offset, uint64_t d, uint64_t k_max, int64_t numesign, uint64_t den0,
                      uint64_t den1)
 {
+    CBL_GUARD_BEGIN
     return sglobal(c, offset, d, k_max, numesign, den0, den1, 1ull << 32);
+    CBL_GUARD_END
 }
 
 int cbl_Sglobal64mtg(cbl_ctx *c, uint64_t offset, uint64_t d, uint64_t k_max, int64_t numesign, uint64_t den0,
                      uint64_t den1)
 {
+    CBL_GUARD_BEGIN
     return sglobal(c, offset, d, k_max, numesign, den0, den1, kW2XMax);
+    CBL_GUARD_END
 }
 
 int cbl_Sglobal_after(cbl_ctx *c, uint64_t d, int64_t numesign, uint64_t den0, uint64_t den1)
 {
+    CBL_GUARD_BEGIN
     if (!c || !series_ok(den0, den1) || (numesign != 0 && numesign != 1)) return CBL_E_ARG;
     cudaSetDevice(c->device);
     if (is192(c)) {
@@ -535,20 +569,24 @@ int cbl_Sglobal_after(cbl_ctx *c, uint64_t d, int64_t numesign, uint64_t den0, u
     CK(launch_dd_tail(c->d_bigsum, d, (int)numesign, (uint32_t)den0, (uint32_t)den1, c->st));
     c->launches++;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_Ssum(cbl_ctx *c)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     cudaSetDevice(c->device);
     if (is192(c)) CK(launch_ssum192(c->d_slots, c->d_partial, c->st));
     else CK(launch_dd_ssum(c->d_bigsum, kDDBlocks, c->d_ddpartial, c->st));
     c->launches++;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_Sum7(cbl_ctx *c, uint64_t numer)
 {
+    CBL_GUARD_BEGIN
     if (!c || numer == 0 || (numer & (numer - 1)) != 0 || numer > 256) return CBL_E_ARG;
     cudaSetDevice(c->device);
     int sh = 0;
@@ -557,10 +595,12 @@ int cbl_Sum7(cbl_ctx *c, uint64_t numer)
     else CK(launch_dd_sum7(c->d_ddpartial, c->d_ddans, (int)numer, c->st));
     c->launches++;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_BatchCalc(cbl_ctx *c, uint64_t k_start, uint64_t k_end, int f, uint64_t d)
 {
+    CBL_GUARD_BEGIN
     if (!c || !formula_ok(f)) return CBL_E_ARG;
     cudaSetDevice(c->device);
     const uint64_t kend = std::min(k_end, d);
@@ -588,16 +628,20 @@ int cbl_BatchCalc(cbl_ctx *c, uint64_t k_start, uint64_t k_end, int f, uint64_t 
         }
     }
     return cbl_Ssum(c);
+    CBL_GUARD_END
 }
 
 int cbl_AddAns(cbl_ctx *c, int f)
 {
+    CBL_GUARD_BEGIN
     if (!formula_ok(f)) return CBL_E_ARG;
     return cbl_Sum7(c, (uint64_t)kNumer[f]);
+    CBL_GUARD_END
 }
 
 int cbl_read_partial(cbl_ctx *c, void *out)
 {
+    CBL_GUARD_BEGIN
     if (!c || !out) return CBL_E_ARG;
     cudaSetDevice(c->device);
     if (is192(c)) CK(cudaMemcpyAsync(c->h_small, c->d_partial, 24, cudaMemcpyDeviceToHost, c->st));
@@ -606,10 +650,12 @@ int cbl_read_partial(cbl_ctx *c, void *out)
     if (rc) return rc;
     std::memcpy(out, c->h_small, is192(c) ? 24 : 16);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_read_ans(cbl_ctx *c, void *out)
 {
+    CBL_GUARD_BEGIN
     if (!c || !out) return CBL_E_ARG;
     cudaSetDevice(c->device);
     if (is192(c)) CK(cudaMemcpyAsync(c->h_small, c->d_ans, 24, cudaMemcpyDeviceToHost, c->st));
@@ -618,10 +664,12 @@ int cbl_read_ans(cbl_ctx *c, void *out)
     if (rc) return rc;
     std::memcpy(out, c->h_small, is192(c) ? 24 : 16);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_query(cbl_ctx *c)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     const cudaError_t e = cudaStreamQuery(c->st);
     if (e == cudaSuccess) return 0;
@@ -630,10 +678,12 @@ int cbl_query(cbl_ctx *c)
         return 1;
     }
     return CBL_E_CUDA;
+    CBL_GUARD_END
 }
 
 int cbl_wait(cbl_ctx *c, int timeout_ms)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     const auto t0 = std::chrono::steady_clock::now();
     for (;;) {
@@ -645,6 +695,7 @@ int cbl_wait(cbl_ctx *c, int timeout_ms)
         }
         std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
+    CBL_GUARD_END
 }
 
 static uint64_t fnv1a(const void *p, size_t n, uint64_t h = 1469598103934665603ull)
@@ -785,16 +836,19 @@ static int compute_d(cbl_ctx *c, uint64_t d, int shift, char hex[49])
 
 int cbl_compute(cbl_ctx *c, uint64_t needD, char hex[49])
 {
+    CBL_GUARD_BEGIN
     if (!c || !hex) return CBL_E_ARG;
     uint64_t d;
     int rc = cbl_pos_to_d(needD, &d, nullptr);
     if (rc) return rc;
     cudaSetDevice(c->device);
     return compute_d(c, d, 0, hex);
+    CBL_GUARD_END
 }
 
 int cbl_compute_hexpos(cbl_ctx *c, uint64_t p, char hex[49])
 {
+    CBL_GUARD_BEGIN
     if (!c || !hex) return CBL_E_ARG;
     if (p < 3 || p > kMaxNeedD) return CBL_E_POSITION;
     const uint64_t B = 4 * (p - 1);
@@ -802,10 +856,12 @@ int cbl_compute_hexpos(cbl_ctx *c, uint64_t p, char hex[49])
     const int shift = (int)((B - 6) - 10 * d);
     cudaSetDevice(c->device);
     return compute_d(c, d, shift, hex);
+    CBL_GUARD_END
 }
 
 int cbl_run_job(cbl_ctx *c, uint64_t needD, int s, uint64_t b, uint64_t batchsize, char hex[49])
 {
+    CBL_GUARD_BEGIN
     if (!c || !hex || !formula_ok(s) || batchsize == 0) return CBL_E_ARG;
     uint64_t d;
     int rc = cbl_pos_to_d(needD, &d, nullptr);
@@ -828,6 +884,7 @@ int cbl_run_job(cbl_ctx *c, uint64_t needD, int s, uint64_t b, uint64_t batchsiz
         if (!rc) dd_to_hex(a[0], a[1], hex);
     }
     return rc;
+    CBL_GUARD_END
 }
 
 // ---- balanced work-mode planning
@@ -880,6 +937,7 @@ static double range_cost(uint64_t d, int f, uint64_t k0, uint64_t k1)
 
 int cbl_plan_jobs(uint64_t needD, int njobs, int *out_s, uint64_t *out_k0, uint64_t *out_k1, int cap)
 {
+    CBL_GUARD_BEGIN
     if (njobs < 7 || cap < njobs || !out_s || !out_k0 || !out_k1) return CBL_E_ARG;
     uint64_t d;
     int rc = cbl_pos_to_d(needD, &d, nullptr);
@@ -924,10 +982,12 @@ int cbl_plan_jobs(uint64_t needD, int njobs, int *out_s, uint64_t *out_k0, uint6
         }
     }
     return n;
+    CBL_GUARD_END
 }
 
 int cbl_run_job_range(cbl_ctx *c, uint64_t needD, int s, uint64_t k0, uint64_t k1, char hex[49])
 {
+    CBL_GUARD_BEGIN
     if (!c || !hex || !formula_ok(s) || k1 < k0) return CBL_E_ARG;
     uint64_t d;
     int rc = cbl_pos_to_d(needD, &d, nullptr);
@@ -948,10 +1008,12 @@ int cbl_run_job_range(cbl_ctx *c, uint64_t needD, int s, uint64_t k0, uint64_t k
         if (!rc) dd_to_hex(a[0], a[1], hex);
     }
     return rc;
+    CBL_GUARD_END
 }
 
 int cbl_workmode_sum(const char *const *hex48, int n, char out[49])
 {
+    CBL_GUARD_BEGIN
     if (!out || n < 0 || (n > 0 && !hex48)) return CBL_E_ARG;
     int acc[48] = {0};
     for (int j = 0; j < n; ++j) {
@@ -970,11 +1032,13 @@ int cbl_workmode_sum(const char *const *hex48, int n, char out[49])
     for (int i = 0; i < 48; ++i) out[i] = hx[acc[i]];
     out[48] = 0;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_job_write(const char *workdir, int s, uint64_t b, const char *hex, int deviceno, const char *devname,
                   int64_t ms)
 {
+    CBL_GUARD_BEGIN
     if (!workdir || !hex || !formula_ok(s)) return CBL_E_ARG;
     char dir[32];
     std::snprintf(dir, sizeof dir, "/%d", s);
@@ -998,10 +1062,12 @@ int cbl_job_write(const char *workdir, int s, uint64_t b, const char *hex, int d
         return CBL_E_IO;
     }
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_job_read(const char *workdir, int s, uint64_t b, char hex[49])
 {
+    CBL_GUARD_BEGIN
     if (!workdir || !hex || !formula_ok(s)) return CBL_E_ARG;
     const std::string p = job_path(workdir, s, b);
     FILE *f = std::fopen(p.c_str(), "rb");
@@ -1015,10 +1081,12 @@ int cbl_job_read(const char *workdir, int s, uint64_t b, char hex[49])
     std::memcpy(hex, line, 48);
     hex[48] = 0;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_workdir_sum(const char *workdir, char out[49], int counts[7])
 {
+    CBL_GUARD_BEGIN
     if (!workdir || !out) return CBL_E_ARG;
     std::vector<std::string> hs;
     for (int s = 0; s < 7; ++s) {
@@ -1038,10 +1106,12 @@ int cbl_workdir_sum(const char *workdir, char out[49], int counts[7])
     std::vector<const char *> ptrs;
     for (auto &h : hs) ptrs.push_back(h.c_str());
     return cbl_workmode_sum(ptrs.data(), (int)ptrs.size(), out);
+    CBL_GUARD_END
 }
 
 int cbl_batch(cbl_ctx *c, const uint64_t *pos, int n, uint64_t *out3n)
 {
+    CBL_GUARD_BEGIN
     if (!c || (n > 0 && (!pos || !out3n)) || n < 0) return CBL_E_ARG;
     if (!is192(c)) return CBL_E_PRECISION;
     if (n == 0) return CBL_OK;
@@ -1059,10 +1129,12 @@ int cbl_batch(cbl_ctx *c, const uint64_t *pos, int n, uint64_t *out3n)
     if (rc) return rc;
     std::memcpy(out3n, c->h_out3, sizeof(uint64_t) * 3 * n);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_terms(cbl_ctx *c, uint64_t d, int f, const uint64_t *k, int n, uint64_t *out3n)
 {
+    CBL_GUARD_BEGIN
     if (!c || !formula_ok(f) || n < 0 || (n > 0 && (!k || !out3n))) return CBL_E_ARG;
     if (n == 0) return CBL_OK;
     for (int i = 0; i < n; ++i)
@@ -1081,10 +1153,12 @@ int cbl_terms(cbl_ctx *c, uint64_t d, int f, const uint64_t *k, int n, uint64_t 
     c->launches++;
     CK(cudaMemcpyAsync(out3n, d_out, sizeof(uint64_t) * 3 * n, cudaMemcpyDeviceToHost, c->st));
     return sync(c);
+    CBL_GUARD_END
 }
 
 int cbl_prepare(cbl_ctx *c, const uint64_t *pos, int n)
 {
+    CBL_GUARD_BEGIN
     if (!c || n <= 0 || !pos) return CBL_E_ARG;
     if (!is192(c)) return CBL_E_PRECISION;
     std::vector<uint64_t> d(n);
@@ -1095,17 +1169,21 @@ int cbl_prepare(cbl_ctx *c, const uint64_t *pos, int n)
     }
     cudaSetDevice(c->device);
     return prepare_positions(c, d.data(), sh.data(), n);
+    CBL_GUARD_END
 }
 
 int cbl_run_prepared(cbl_ctx *c)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     cudaSetDevice(c->device);
     return launch_prepared(c);
+    CBL_GUARD_END
 }
 
 int cbl_read_results(cbl_ctx *c, uint64_t *out3n)
 {
+    CBL_GUARD_BEGIN
     if (!c || !out3n || c->prep_npos <= 0) return CBL_E_ARG;
     cudaSetDevice(c->device);
     const size_t bytes = sizeof(uint64_t) * 3 * c->prep_npos;
@@ -1114,16 +1192,19 @@ int cbl_read_results(cbl_ctx *c, uint64_t *out3n)
     if (rc) return rc;
     std::memcpy(out3n, c->h_out3, bytes);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_prepared_info(const cbl_ctx *c, uint64_t *terms, uint64_t *tiles, int *segments, int *grid)
 {
+    CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     if (terms) *terms = c->prep_terms;
     if (tiles) *tiles = c->prep_ntiles;
     if (segments) *segments = c->prep_nseg;
     if (grid) *grid = grid_192(const_cast<cbl_ctx *>(c));
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 // ---- autotuning: tile size x persistent CTAs per SM, timed on the caller's
@@ -1167,6 +1248,7 @@ static void tune_cache_store(const std::string &key, int tile, int ctas)
 
 int cbl_autotune(cbl_ctx *c, const uint64_t *pos, int n, int force, int *best_tile, int *best_ctas, double *best_ms)
 {
+    CBL_GUARD_BEGIN
     if (!c || !pos || n <= 0) return CBL_E_ARG;
     if (!is192(c)) return CBL_E_PRECISION;
     cudaSetDevice(c->device);
@@ -1208,10 +1290,12 @@ int cbl_autotune(cbl_ctx *c, const uint64_t *pos, int n, int force, int *best_ti
     if (best_ctas) *best_ctas = ctas;
     if (best_ms) *best_ms = ms_best;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_run_prepared_budget(cbl_ctx *c, double budget_ms, uint64_t *tiles_done, uint64_t *tiles_total)
 {
+    CBL_GUARD_BEGIN
     if (!c || budget_ms <= 0 || c->prep_npos <= 0) return CBL_E_ARG;
     cudaSetDevice(c->device);
     const int n = c->prep_npos;
@@ -1236,6 +1320,7 @@ int cbl_run_prepared_budget(cbl_ctx *c, double budget_ms, uint64_t *tiles_done, 
     if (tiles_done) *tiles_done = done;
     if (tiles_total) *tiles_total = c->prep_ntiles;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 // Checkpoint of a budgeted run: header, tiles done, the slots' digit sums.
@@ -1252,6 +1337,7 @@ int64_t cbl_checkpoint_size(const cbl_ctx *c)
 
 int cbl_checkpoint_save(cbl_ctx *c, void *buf, int64_t size)
 {
+    CBL_GUARD_BEGIN
     if (!c || !buf || c->prep_npos <= 0 || size < cbl_checkpoint_size(c)) return CBL_E_ARG;
     cudaSetDevice(c->device);
     int rc = sync(c);
@@ -1268,10 +1354,12 @@ int cbl_checkpoint_save(cbl_ctx *c, void *buf, int64_t size)
     else
         std::memset(static_cast<char *>(buf) + sizeof h, 0, sizeof(unsigned long long) * 6 * 7 * c->prep_npos);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_checkpoint_load(cbl_ctx *c, const void *buf, int64_t size)
 {
+    CBL_GUARD_BEGIN
     if (!c || !buf || c->prep_npos <= 0 || size < cbl_checkpoint_size(c)) return CBL_E_ARG;
     CkptHeader h;
     std::memcpy(&h, buf, sizeof h);
@@ -1285,19 +1373,23 @@ int cbl_checkpoint_load(cbl_ctx *c, const void *buf, int64_t size)
     CK(cudaMemcpy(c->d_counter, &done, sizeof done, cudaMemcpyHostToDevice));
     c->partial = 1;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_kernel_ms(cbl_ctx *c, float *ms)
 {
+    CBL_GUARD_BEGIN
     if (!c || !ms || !c->ev_valid) return CBL_E_ARG;
     cudaSetDevice(c->device);
     CK(cudaEventSynchronize(c->ev_k1));
     CK(cudaEventElapsedTime(ms, c->ev_k0, c->ev_k1));
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_probe_imad(cbl_ctx *c, int iters, double *ops_per_s, double *ms)
 {
+    CBL_GUARD_BEGIN
     if (!c || iters <= 0) return CBL_E_ARG;
     cudaSetDevice(c->device);
     uint32_t *d_sink = nullptr;
@@ -1326,11 +1418,13 @@ int cbl_probe_imad(cbl_ctx *c, int iters, double *ops_per_s, double *ms)
     if (ms) *ms = best;
     if (ops_per_s) *ops_per_s = (double)ops / (best * 1e-3);
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 // ---- HSP-friendly pointer forms
 int cbl_pos_to_d_p(const int64_t *needD, int64_t *d, int64_t *needD_adj)
 {
+    CBL_GUARD_BEGIN
     if (!needD || *needD < 0) return CBL_E_ARG;
     uint64_t a, b;
     const int rc = cbl_pos_to_d((uint64_t)*needD, &a, &b);
@@ -1338,24 +1432,31 @@ int cbl_pos_to_d_p(const int64_t *needD, int64_t *d, int64_t *needD_adj)
     if (d) *d = (int64_t)a;
     if (needD_adj) *needD_adj = (int64_t)b;
     return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_compute_p(cbl_ctx *c, const int64_t *needD, char hex[49])
 {
+    CBL_GUARD_BEGIN
     if (!needD || *needD < 0) return CBL_E_ARG;
     return cbl_compute(c, (uint64_t)*needD, hex);
+    CBL_GUARD_END
 }
 
 int cbl_BatchCalc_p(cbl_ctx *c, const int64_t *k_start, const int64_t *k_end, int f, const int64_t *d)
 {
+    CBL_GUARD_BEGIN
     if (!k_start || !k_end || !d || *k_start < 0 || *k_end < 0 || *d < 0) return CBL_E_ARG;
     return cbl_BatchCalc(c, (uint64_t)*k_start, (uint64_t)*k_end, f, (uint64_t)*d);
+    CBL_GUARD_END
 }
 
 int cbl_run_job_p(cbl_ctx *c, const int64_t *needD, int s, const int64_t *b, const int64_t *batchsize, char hex[49])
 {
+    CBL_GUARD_BEGIN
     if (!needD || !b || !batchsize || *needD < 0 || *b < 0 || *batchsize <= 0) return CBL_E_ARG;
     return cbl_run_job(c, (uint64_t)*needD, s, (uint64_t)*b, (uint64_t)*batchsize, hex);
+    CBL_GUARD_END
 }
 
 }  // extern "C"
