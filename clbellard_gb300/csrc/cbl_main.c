@@ -3,7 +3,10 @@
  * CLBellard.exe (normal mode and work mode, Bellard_192.hsp) and
  * workmodeSum0_6.exe (workmodeSum0_6.hsp) without the GUI.
  *
- *   cbl normal <digits> [precision 0|1|2] [device]
+ *   cbl normal <digits> [precision 0|1|2] [device] [--json] [--check]
+ *       --json   one JSON line: position, d, mode, terms, seconds, terms/s, hex
+ *       --check  also computes hex position P-8 and reports how many of the
+ *                overlapping hex digits agree (192-bit modes)
  *   cbl work   <worklist.txt> [workdir] [device]
  *   cbl sum    [workdir]
  *   cbl hexpos <p> [device]            any hex position p >= 3
@@ -48,23 +51,55 @@ static uint64_t parse_digits(const char *s)
     return any ? v : 0;
 }
 
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 static int cmd_normal(int argc, char **argv)
 {
-    if (argc < 3) return fprintf(stderr, "usage: cbl normal <digits> [precision] [device]\n"), 2;
-    uint64_t needD = parse_digits(argv[2]), d, adj;
-    int precision = argc > 3 ? atoi(argv[3]) : 1, device = argc > 4 ? atoi(argv[4]) : 0;
+    int json = 0, check = 0, npos = 0;
+    const char *pos[3] = {NULL, NULL, NULL};              /* digits, precision, device */
+    for (int i = 2; i < argc; ++i) {
+        if (!strcmp(argv[i], "--json")) json = 1;
+        else if (!strcmp(argv[i], "--check")) check = 1;
+        else if (npos < 3) pos[npos++] = argv[i];
+    }
+    if (!pos[0]) return fprintf(stderr, "usage: cbl normal <digits> [precision] [device] [--json] [--check]\n"), 2;
+    uint64_t needD = parse_digits(pos[0]), d, adj;
+    int precision = pos[1] ? atoi(pos[1]) : 1, device = pos[2] ? atoi(pos[2]) : 0;
     int rc = cbl_pos_to_d(needD, &d, &adj);
     if (rc) return fail(rc, "invalid digits");
     cbl_ctx *c;
     if ((rc = cbl_create(device, precision, &c))) return fail(rc, "cbl_create");
-    char name[256], hex[49];
+    char name[256], hex[49], hex8[49];
     cbl_device_name(c, name, sizeof name);
-    printf("%s\ndigits=%llu\nloopnum=%llu\n", name, (unsigned long long)adj, (unsigned long long)d);
-    const int64_t t0 = now_ms();
+    if (!json) printf("%s\ndigits=%llu\nloopnum=%llu\n", name, (unsigned long long)adj, (unsigned long long)d);
+    const double t0 = now_s();
     rc = cbl_compute(c, needD, hex);
-    const int64_t t1 = now_ms();
+    const double t1 = now_s();
     if (rc) return cbl_destroy(c), fail(rc, "cbl_compute");
-    printf("All calc time %lldms\nPI value output -> \n%s\n", (long long)(t1 - t0), hex);
+    /* overlap: hex digit i of position P is digit i+8 of position P-8 */
+    int overlap = -1;
+    if (check && precision != 0 && adj > 10) {
+        rc = cbl_compute_hexpos(c, adj - 8, hex8);
+        if (rc) return cbl_destroy(c), fail(rc, "cbl_compute_hexpos");
+        overlap = 0;
+        while (overlap < 40 && hex[overlap] == hex8[overlap + 8]) ++overlap;
+    }
+    if (json) {
+        printf("{\"position\": %llu, \"d\": %llu, \"mode\": %d, \"terms\": %llu, \"seconds\": %.6f, "
+               "\"terms_per_s\": %.6g, \"hex\": \"%s\", \"device\": \"%s\"",
+               (unsigned long long)adj, (unsigned long long)d, precision, (unsigned long long)(7 * d), t1 - t0,
+               7.0 * (double)d / (t1 - t0), hex, name);
+        if (overlap >= 0) printf(", \"overlap_digits\": %d", overlap);
+        printf("}\n");
+    } else {
+        printf("All calc time %lldms\nPI value output -> \n%s\n", (long long)((t1 - t0) * 1000.0), hex);
+        if (overlap >= 0) printf("hex digits agreeing with position %llu: %d\n", (unsigned long long)(adj - 8), overlap);
+    }
     cbl_destroy(c);
     return 0;
 }

@@ -21,6 +21,18 @@ def test_normal_mode():
     assert "loopnum=399999" in out
 
 
+def test_normal_mode_json_and_overlap_check():
+    """One JSON line per run; --check recomputes position P-8 and counts the
+    agreeing overlap digits (no oracle in the product)."""
+    import json
+    out = subprocess.run([driver(), "normal", "10000000", "1", "--json", "--check"], capture_output=True, text=True,
+                         check=True).stdout
+    rec = json.loads(out.strip().splitlines()[-1])
+    assert rec["hex"] == load_golden("oracle_small.json")["10000000"]["hex192"]
+    assert rec["position"] == 10000000 and rec["d"] == 3999999 and rec["terms"] == 7 * 3999999
+    assert rec["overlap_digits"] >= 28 and rec["terms_per_s"] > 0
+
+
 def test_work_mode_and_merge(tmp_path):
     wl = tmp_path / "worklist.txt"
     # the reference's worklist layout (work/worklist_sample.txt), CR LF line ends
