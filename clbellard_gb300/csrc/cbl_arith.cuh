@@ -18,7 +18,7 @@
 //   width 1 (m < 2^28): R = 2^32, residues kept lazily in [0, 4m).
 //   middle width 1 (2^28 <= m < 2^31): R = 2^32, residues in [0, m).
 //   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m), carries kept.
-//   short width 2 (2^32 <= m < 2^40): R = 2^64, residues in [0, 4m).
+//   short width 2 (2^32 <= m < 2^44): R = 2^64, residues in [0, 4m).
 //   width 2 (2^28 <= m < 2^60): R = 2^64 by two word steps, residues in [0, 4m).
 //   wide width 2 (2^60 <= m < 2^62): the same steps with residues in [0, 2m).
 // The ladder step is y <- REDC(y^2) << b with b the next exponent bit; in the
@@ -361,14 +361,15 @@ __device__ __forceinline__ uint64_t w2_pow2(uint64_t E, uint64_t m, uint32_t mp)
     return r;
 }
 
-// --------------------------------------------------- width 2, m < 2^40 --
-// 2^32 <= m < 2^40 (m1 < 2^8), y in [0,4m) (y1 < 2^10). Same REDC_2^64 as
+// --------------------------------------------------- width 2, m < 2^44 --
+// 2^32 <= m < 2^44 (m1 < 2^12), y in [0,4m) (y1 < 2^14). Same REDC_2^64 as
 // w2_sqr over the short top words: y^2 = y0^2 + y0 (2 y1) 2^32 + y1^2 2^64
-// with y0 (2 y1) < 2^43 and y1^2 < 2^20, so word step 1 is
-//   s = (y0^2 + u0 m0) / 2^32 + y1^2 2^32 + y0 (2 y1) + u0 m1 < 2^54,
-// one carry chain whose carry out of the first multiply-add lands on y1^2;
-// word step 2 is z = (s + u1 m0) / 2^32 + u1 m1 < 2m with its carry out
-// placed in the high word.
+// with y0 (2 y1) < 2^47 and y1^2 < 2^28, so word step 1 is
+//   s = (y0^2 + u0 m0) / 2^32 + y1^2 2^32 + y0 (2 y1) + u0 m1 < 2^61,
+// one carry chain whose carry out of the first multiply-add lands on y1^2
+// (its high words stay below 2^29 and 2^30: no carry leaves the chain);
+// word step 2 is z = (s + u1 m0) / 2^32 + u1 m1 < m + 2^29 < 2m with its
+// carry out placed in the high word. (The chain holds up to m < 2^46.)
 __device__ __forceinline__ void w2s_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0, uint32_t m1, uint32_t mp,
                                         uint32_t b)
 {
@@ -407,8 +408,9 @@ struct W2SState {
     __device__ __forceinline__ void step(uint32_t b) { w2s_sqr(y0, y1, m0, m1, mp, b); }
 };
 
-// A value in (0, 2m) congruent to 2^(64 + p), 1 <= p <= 7, for 2^32 <= m < 2^40:
-// |2^(64+p) - q1 m| <= 2^(43+p) + m and |r1/m| <= 2^18, so two rounds suffice.
+// A value in (0, 2m) congruent to 2^(64 + p), 1 <= p <= 7, for 2^32 <= m < 2^44:
+// |2^(64+p) - q1 m| <= 2^(43+p) + m and |r1/m| <= 2^18, so two rounds suffice
+// (the products stay below 2^62).
 __device__ __forceinline__ uint64_t w2s_start(uint64_t m, uint32_t p)
 {
     const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
@@ -423,7 +425,7 @@ __device__ __forceinline__ uint64_t w2s_start(uint64_t m, uint32_t p)
     return (uint64_t)(r1 + (int64_t)(1 - q2) * (int64_t)m);
 }
 
-// r6 = 2^E mod m in [0, m) for E >= 65, 2^32 <= m < 2^40. The start value
+// r6 = 2^E mod m in [0, m) for E >= 65, 2^32 <= m < 2^44. The start value
 // takes the leading up-to-three bits of E - 64 at once.
 __device__ __forceinline__ uint64_t w2s_pow2(uint64_t E, uint64_t m, uint32_t mp)
 {

@@ -163,7 +163,7 @@ bool series_ok(uint64_t den0, uint64_t den1)
 }
 
 // Append the segments covering k in [k0, k1) of one series, split at d (main
-// vs tail) and at the residue-kind boundaries m = 2^28, 2^31, 2^32, 2^40 and 2^60. k = 0 with
+// vs tail) and at the residue-kind boundaries m = 2^28, 2^31, 2^32, 2^44 and 2^60. k = 0 with
 // den1 = 1 (m = 1) contributes exactly 0 and is left out.
 int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, int sign, uint32_t slot,
                  uint64_t k0, uint64_t k1)
@@ -174,7 +174,7 @@ int add_segments(std::vector<Seg> &v, uint64_t d, uint32_t den0, uint32_t den1, 
     const uint64_t kw1 = (kW1Max - den1 + den0 - 1) / den0;    // first k with m >= 2^28
     const uint64_t kw1m = (kW1MMax - den1 + den0 - 1) / den0;  // first k with m >= 2^31
     const uint64_t kw1s = (kW1SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^32
-    const uint64_t kw2s = (kW2SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^40
+    const uint64_t kw2s = (kW2SMax - den1 + den0 - 1) / den0;  // first k with m >= 2^44
     const uint64_t kw2 = (kW2Max - den1 + den0 - 1) / den0;    // first k with m >= 2^60
     std::vector<uint64_t> pts = {k0, k1};
     for (uint64_t c : {d, kw1, kw1m, kw1s, kw2s, kw2}) pts.push_back(std::min(std::max(c, k0), k1));

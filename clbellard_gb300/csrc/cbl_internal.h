@@ -17,7 +17,7 @@ constexpr uint32_t kDen1[7] = {1, 3, 1, 3, 5, 7, 9};
 constexpr uint64_t kW1Max = 1ull << 28;   // width 1 (one 32-bit word) for m < 2^28
 constexpr uint64_t kW1MMax = 1ull << 31;  // middle width 1 for 2^28 <= m < 2^31
 constexpr uint64_t kW1SMax = 1ull << 32;  // strict width 1 for 2^31 <= m < 2^32
-constexpr uint64_t kW2SMax = 1ull << 40;  // short width 2 for 2^32 <= m < 2^40
+constexpr uint64_t kW2SMax = 1ull << 44;  // short width 2 for 2^32 <= m < 2^44
 constexpr uint64_t kW2Max = 1ull << 60;   // width 2 (two words, residues < 4m) for m < 2^60
 constexpr uint64_t kW2XMax = 1ull << 62;  // wide width 2 (residues < 2m) for 2^60 <= m < 2^62
 constexpr uint64_t kDDMax = 1ull << 53;   // double-double mode: m and r exact as doubles below, double-doubles above

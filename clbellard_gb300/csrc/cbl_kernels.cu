@@ -49,7 +49,7 @@ __device__ __forceinline__ void shr192(uint32_t q[6], int s)
 // One term's six quotient digits: k < d gives frac(2^(10(d-k))/m), k >= d the
 // tail value 2^(-10(k-d))/m (digits of 1/m shifted right by 10(k-d)).
 // KIND: 1 = width 1 (m < 2^28), 5 = middle width 1 (2^28 <= m < 2^31),
-// 3 = strict width 1 (2^28 <= m < 2^32), 4 = short width 2 (2^32 <= m < 2^40),
+// 3 = strict width 1 (2^28 <= m < 2^32), 4 = short width 2 (2^32 <= m < 2^44),
 // 2 = width 2 (2^28 <= m < 2^60), 6 = wide width 2 (2^60 <= m < 2^62).
 template <int KIND, bool TAIL>
 __device__ __forceinline__ void term_digits(uint64_t d, uint64_t k, uint64_t m, uint32_t q[6])

@@ -52,12 +52,23 @@ def test_terms_32bit_boundary(ctx192, oracle, f):
 
 
 @pytest.mark.parametrize("f", range(7))
-def test_terms_40bit_boundary(ctx192, oracle, f):
-    """k around the first modulus >= 2^40 (short width 2 -> width 2)."""
+def test_terms_40bit(ctx192, oracle, f):
+    """k around m = 2^40, inside the short width-2 kind (its top words up to
+    2^8 / 2^10 there), and the last terms of position 1e12."""
     den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
     k40 = ((1 << 40) - den1 + den0 - 1) // den0
     d = 399999999999
     check_terms(ctx192, oracle, d, f, list(range(k40 - 40, k40 + 40)) + list(range(d - 40, d + 20)))
+
+
+@pytest.mark.parametrize("f", range(7))
+def test_terms_44bit_boundary(ctx192, oracle, f):
+    """k around the first modulus >= 2^44 (short width 2 -> width 2), where
+    the short kind's top words are largest, and the last terms below d."""
+    den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
+    k44 = ((1 << 44) - den1 + den0 - 1) // den0
+    d = 39999999999999
+    check_terms(ctx192, oracle, d, f, list(range(k44 - 60, k44 + 40)) + list(range(d - 40, d + 20)))
 
 
 def test_terms_sampled_1e8(ctx192, oracle):
