@@ -25,12 +25,22 @@ def test_terms_small_positions(ctx192, oracle, f):
 
 @pytest.mark.parametrize("f", range(7))
 def test_terms_width_boundary(ctx192, oracle, f):
-    """k around the first modulus >= 2^28 (width 1 -> width 2)."""
+    """k around the first modulus >= 2^28 (width 1 -> middle width 1)."""
     den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
     kw = (W1_MAX - den1 + den0 - 1) // den0
     d = 3999999999
     ks = list(range(kw - 40, kw + 40))
     check_terms(ctx192, oracle, d, f, ks)
+
+
+@pytest.mark.parametrize("f", range(7))
+def test_terms_30bit(ctx192, oracle, f):
+    """k around m = 2^30 inside the middle width-1 kind, with d just either
+    side so the tails fall there too."""
+    den0, den1 = oracle.DEN0[f], oracle.DEN1[f]
+    k30 = ((1 << 30) - den1 + den0 - 1) // den0
+    for d in (3999999999, k30 - 7, k30 + 3):
+        check_terms(ctx192, oracle, d, f, [k for k in range(k30 - 40, k30 + 40) if k < d + 20])
 
 
 @pytest.mark.parametrize("f", range(7))
