@@ -3,6 +3,12 @@ measured pass) and print the result and the term-kernel time. Small enough to
 run under a profiler:
 
     python -m clbellard_gb300.profile_case --position 1000000000
+
+With --range f k0 k1, run instead one series' BatchCalc over k in [k0, k1)
+at the position's d (twice), e.g. a range where one residue kind does all
+the work:
+
+    python -m clbellard_gb300.profile_case --position 10000000000 --range 0 3000000000 3100000000
 """
 from __future__ import annotations
 
@@ -17,8 +23,23 @@ def main():
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--ctas", type=int, default=0)
+    ap.add_argument("--range", type=int, nargs=3, metavar=("F", "K0", "K1"))
     args = ap.parse_args()
-    with C.Context(args.device, 1) as ctx:
+    if args.range:
+        import time
+        f, k0, k1 = args.range
+        d, _ = C.pos_to_d(args.position)
+        with C.Context(args.device, 1) as ctx:
+            if args.tile:
+                ctx.set_tuning(args.tile, args.ctas)
+            for _ in range(2):
+                ctx.Set0mem()
+                t0 = time.perf_counter()
+                ctx.BatchCalc(k0, k1, f, d)
+                ctx.wait()
+                ms = (time.perf_counter() - t0) * 1e3
+            print("%048x %.3f ms (%d terms, wall)" % (ctx.read_partial(), ms, k1 - k0))
+        return
         if args.tile:
             ctx.set_tuning(args.tile, args.ctas)
         ctx.prepare([args.position])
