@@ -155,3 +155,21 @@ def test_two_rank_gloo_merge(oracle):
     d, _ = oracle.pos_to_d(needD)
     want = oracle.to_hex(oracle.result(d, 0, 3), 3)
     assert res[0] == res[1] == want
+
+
+def test_driver_plan_worklist(cbl, oracle):
+    """`cbl plan` (no GPU needed) prints a worklist the parser reads back: the
+    reference's header lines, then `s_b k0 k1` lines tiling each series."""
+    import subprocess
+    from clbellard_gb300 import build
+    from clbellard_gb300 import workmode as W
+    out = subprocess.run([build.DRIVER, "plan", "1000000", "20"], capture_output=True, text=True, check=True).stdout
+    wl = W.parse_worklist(out)
+    d, _ = oracle.pos_to_d(1000000)
+    assert wl.digits == 1000000 and wl.precision == 1 and len(wl.jobs) == 20
+    assert [(s, k0, k1) for (s, _), (k0, k1) in wl.ranges.items()] == cbl.plan_jobs(1000000, 20)
+    for s in range(7):
+        rs = sorted(r for (f, _), r in wl.ranges.items() if f == s)
+        assert rs[0][0] == 0 and rs[-1][1] == d + 20 and all(a[1] == b[0] for a, b in zip(rs, rs[1:]))
+    r = subprocess.run([build.DRIVER, "plan", "1000000", "3"], capture_output=True, text=True)
+    assert r.returncode != 0
