@@ -408,9 +408,12 @@ struct W2SState {
     __device__ __forceinline__ void step(uint32_t b) { w2s_sqr(y0, y1, m0, m1, mp, b); }
 };
 
-// A value in (0, 2m) congruent to 2^(64 + p), 1 <= p <= 7, for 2^32 <= m < 2^44:
-// |2^(64+p) - q1 m| <= 2^(43+p) + m and |r1/m| <= 2^18, so two rounds suffice
-// (the products stay below 2^62).
+// A value in (0, 2m) congruent to 2^(64 + p), 1 <= p <= 15, for 2^32 <= m < 2^44:
+// q1 = trunc(2^(64+p) / m) from a float reciprocal leaves |r1| <= 2^(43+p) + m
+// (< 2^59); q2 = rint(r1 / m) (|q2| <= 2^27) is off by a few units, so
+// |r2| <= ~25m; q3 = rint(r2 / m) is then exact to within one half, and
+// r2 + (1 - q3) m lies in (0, 2m). The q2 m product is taken mod 2^64: r2 is
+// small, so the wrapped difference is exact.
 __device__ __forceinline__ uint64_t w2s_start(uint64_t m, uint32_t p)
 {
     const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
@@ -422,11 +425,15 @@ __device__ __forceinline__ uint64_t w2s_start(uint64_t m, uint32_t p)
     const float fr1 = __fmaf_rn(__int2float_rn((int32_t)(r1 >> 32)), 4294967296.0f,
                                 __uint2float_rn((uint32_t)r1));
     const int32_t q2 = __float2int_rn(fr1 * inv);
-    return (uint64_t)(r1 + (int64_t)(1 - q2) * (int64_t)m);
+    const int64_t r2 = (int64_t)((uint64_t)r1 - (uint64_t)((int64_t)q2 * (int64_t)m));   // exact mod 2^64
+    const float fr2 = __fmaf_rn(__int2float_rn((int32_t)(r2 >> 32)), 4294967296.0f,
+                                __uint2float_rn((uint32_t)r2));
+    const int32_t q3 = __float2int_rn(fr2 * inv);
+    return (uint64_t)(r2 + (int64_t)(1 - q3) * (int64_t)m);
 }
 
 // r6 = 2^E mod m in [0, m) for E >= 65, 2^32 <= m < 2^44. The start value
-// takes the leading up-to-three bits of E - 64 at once.
+// takes the leading up-to-four bits of E - 64 at once.
 __device__ __forceinline__ uint64_t w2s_pow2(uint64_t E, uint64_t m, uint32_t mp)
 {
     const uint64_t Ep = E - 64;
@@ -434,7 +441,7 @@ __device__ __forceinline__ uint64_t w2s_pow2(uint64_t E, uint64_t m, uint32_t mp
     W2SState st{0, 0, (uint32_t)m, (uint32_t)(m >> 32), mp};
     if (hi != 0) {
         const int nb = 32 - __clz(hi);
-        const int t = nb < 3 ? nb : 3;
+        const int t = nb < 4 ? nb : 4;
         const uint64_t y = w2s_start(m, hi >> (nb - t));
         st.y0 = (uint32_t)y;
         st.y1 = (uint32_t)(y >> 32);
@@ -447,7 +454,7 @@ __device__ __forceinline__ uint64_t w2s_pow2(uint64_t E, uint64_t m, uint32_t mp
         for (int i = 31; i >= 0; --i) st.step((lo >> i) & 1u);
     } else {
         const int nb = 32 - __clz(lo);
-        const int t = nb < 3 ? nb : 3;
+        const int t = nb < 4 ? nb : 4;
         const uint64_t y = w2s_start(m, lo >> (nb - t));
         st.y0 = (uint32_t)y;
         st.y1 = (uint32_t)(y >> 32);

@@ -40,6 +40,7 @@ def main():
                 ms = (time.perf_counter() - t0) * 1e3
             print("%048x %.3f ms (%d terms, wall)" % (ctx.read_partial(), ms, k1 - k0))
         return
+    with C.Context(args.device, 1) as ctx:
         if args.tile:
             ctx.set_tuning(args.tile, args.ctas)
         ctx.prepare([args.position])

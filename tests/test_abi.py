@@ -89,6 +89,26 @@ def test_no_device_fails_loudly(cbl):
     assert e.value.code == -3
 
 
+def test_tools_fail_loudly_without_gpu(cbl):
+    """The profiling entry and the driver exit non-zero with the library's
+    no-device error instead of printing nothing or falling back to the CPU."""
+    import sys
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    from clbellard_gb300 import build
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for args in ([], ["--range", "0", "1000", "2000"]):
+        r = subprocess.run([sys.executable, "-m", "clbellard_gb300.profile_case", "--position", "1000000"] + args,
+                           cwd=root, capture_output=True, text=True)
+        assert r.returncode != 0 and "no CUDA device" in r.stderr
+    r = subprocess.run([build.DRIVER, "normal", "1000000"], capture_output=True, text=True)
+    assert r.returncode != 0 and "no CUDA device" in r.stderr
+
+
 def test_driver_binary_built(cbl):
     from clbellard_gb300 import build
     assert os.path.exists(build.DRIVER)
