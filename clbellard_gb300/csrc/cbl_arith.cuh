@@ -73,18 +73,6 @@ __device__ __forceinline__ uint32_t w1_start(uint32_t m)
     return (uint32_t)(r1 + (1 - q2) * (int32_t)m);
 }
 
-// Strict width 1 (2^28 <= m < 2^32): 2^33 mod m in [0, m). q1 <= 32 is off by
-// at most one, so one correction either way suffices.
-__device__ __forceinline__ uint32_t w1s_start(uint32_t m)
-{
-    const float inv = rcp_approx(__uint2float_rn(m));
-    const uint32_t q1 = __float2uint_rz(8589934592.0f * inv);
-    int64_t r = (int64_t)(1ull << 33) - (int64_t)q1 * (int64_t)m;       // in [-m, 2m)
-    r += (r < 0) ? (int64_t)m : 0;
-    r -= (r >= (int64_t)m) ? (int64_t)m : 0;
-    return (uint32_t)r;
-}
-
 // Width 2 (2^28 <= m < 2^62): a value in (0, 2m) congruent to 2^65.
 __device__ __forceinline__ uint64_t w2_start(uint64_t m)
 {
@@ -215,13 +203,6 @@ struct W1SState {
     __device__ __forceinline__ void step(uint32_t b) { y = w1s_sqr(y, m, mp, b); }
 };
 
-// r6 = 2^E mod m in [0, m) for E >= 33 (2^28 <= m < 2^32).
-__device__ __forceinline__ uint32_t w1s_pow2(uint64_t E, uint32_t m, uint32_t mp)
-{
-    W1SState st{w1s_start(m), m, mp};
-    walk_bits(E - 32, st);
-    return st.y;
-}
 
 // ------------------------------------------------------ middle width 1 --
 // 2^28 <= m < 2^31: R = 2^32, residues in [0, m). y^2 + u m < 2^64, so the
@@ -242,8 +223,8 @@ struct W1MState {
     __device__ __forceinline__ void step(uint32_t b) { y = w1m_sqr(y, m, mp, b); }
 };
 
-// 2^(32 + p) mod m in [0, m), 1 <= p <= 7, 2^28 <= m < 2^31: q1 <= 2^11 is off
-// by at most one, so one correction either way suffices.
+// 2^(32 + p) mod m in [0, m), 1 <= p <= 15, 2^28 <= m < 2^32: q1 <= 2^19 is
+// off by at most one, so one correction either way suffices.
 __device__ __forceinline__ uint32_t w1m_start(uint32_t m, uint32_t p)
 {
     const float inv = rcp_approx(__uint2float_rn(m));
@@ -255,15 +236,15 @@ __device__ __forceinline__ uint32_t w1m_start(uint32_t m, uint32_t p)
     return (uint32_t)r;
 }
 
-// Start from the leading up-to-three bits of Ep at once (value p), then walk
-// the rest; st.y is set by start(p).
-template <typename State, typename Start>
-__device__ __forceinline__ void walk_bits_p3(uint64_t Ep, State &st, Start start)
+// Start from the leading up-to-NB bits of Ep at once (value p), then walk the
+// rest; st.y is set by start(p).
+template <int NB, typename State, typename Start>
+__device__ __forceinline__ void walk_bits_start(uint64_t Ep, State &st, Start start)
 {
     const uint32_t hi = (uint32_t)(Ep >> 32), lo = (uint32_t)Ep;
     if (hi != 0) {
         const int nb = 32 - __clz(hi);
-        const int t = nb < 3 ? nb : 3;
+        const int t = nb < NB ? nb : NB;
         start(st, hi >> (nb - t));
         uint32_t h = (nb - t) > 0 ? hi << (32 - (nb - t)) : 0u;
         for (int i = t; i < nb; ++i) {
@@ -274,7 +255,7 @@ __device__ __forceinline__ void walk_bits_p3(uint64_t Ep, State &st, Start start
         for (int i = 31; i >= 0; --i) st.step((lo >> i) & 1u);
     } else {
         const int nb = 32 - __clz(lo);
-        const int t = nb < 3 ? nb : 3;
+        const int t = nb < NB ? nb : NB;
         start(st, lo >> (nb - t));
         uint32_t l = (nb - t) > 0 ? lo << (32 - (nb - t)) : 0u;
         for (int i = t; i < nb; ++i) {
@@ -288,11 +269,25 @@ struct W1MStart {
     __device__ __forceinline__ void operator()(W1MState &st, uint32_t p) const { st.y = w1m_start(st.m, p); }
 };
 
-// r6 = 2^E mod m in [0, m) for E >= 33, 2^28 <= m < 2^31.
+// r6 = 2^E mod m in [0, m) for E >= 33, 2^28 <= m < 2^31. The start value
+// takes the leading up-to-four bits of E - 32 at once.
 __device__ __forceinline__ uint32_t w1m_pow2(uint64_t E, uint32_t m, uint32_t mp)
 {
     W1MState st{0, m, mp};
-    walk_bits_p3(E - 32, st, W1MStart{});
+    walk_bits_start<4>(E - 32, st, W1MStart{});
+    return st.y;
+}
+
+struct W1SStart {
+    __device__ __forceinline__ void operator()(W1SState &st, uint32_t p) const { st.y = w1m_start(st.m, p); }
+};
+
+// r6 = 2^E mod m in [0, m) for E >= 33 (2^31 <= m < 2^32), from the same
+// 4-bit start value.
+__device__ __forceinline__ uint32_t w1s_pow2(uint64_t E, uint32_t m, uint32_t mp)
+{
+    W1SState st{0, m, mp};
+    walk_bits_start<4>(E - 32, st, W1SStart{});
     return st.y;
 }
 
