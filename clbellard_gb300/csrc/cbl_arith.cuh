@@ -113,6 +113,35 @@ __device__ __forceinline__ void walk_bits(uint64_t Ep, State &st)
     }
 }
 
+// Start from the leading up-to-NB bits of Ep at once (value p), then walk the
+// rest; st.y is set by start(p).
+template <int NB, typename State, typename Start>
+__device__ __forceinline__ void walk_bits_start(uint64_t Ep, State &st, Start start)
+{
+    const uint32_t hi = (uint32_t)(Ep >> 32), lo = (uint32_t)Ep;
+    if (hi != 0) {
+        const int nb = 32 - __clz(hi);
+        const int t = nb < NB ? nb : NB;
+        start(st, hi >> (nb - t));
+        uint32_t h = (nb - t) > 0 ? hi << (32 - (nb - t)) : 0u;
+        for (int i = t; i < nb; ++i) {
+            st.step(h >> 31);
+            h <<= 1;
+        }
+#pragma unroll
+        for (int i = 31; i >= 0; --i) st.step((lo >> i) & 1u);
+    } else {
+        const int nb = 32 - __clz(lo);
+        const int t = nb < NB ? nb : NB;
+        start(st, lo >> (nb - t));
+        uint32_t l = (nb - t) > 0 ? lo << (32 - (nb - t)) : 0u;
+        for (int i = t; i < nb; ++i) {
+            st.step(l >> 31);
+            l <<= 1;
+        }
+    }
+}
+
 // ------------------------------------------------- multiply-add chains --
 // Every REDC word step below is written as a PTX carry chain of mad.lo.cc /
 // madc.hi over 32-bit words. A 64-bit multiply-add (mad.wide with a 64-bit
@@ -234,35 +263,6 @@ __device__ __forceinline__ uint32_t w1m_start(uint32_t m, uint32_t p)
     r += (r < 0) ? (int64_t)m : 0;
     r -= (r >= (int64_t)m) ? (int64_t)m : 0;
     return (uint32_t)r;
-}
-
-// Start from the leading up-to-NB bits of Ep at once (value p), then walk the
-// rest; st.y is set by start(p).
-template <int NB, typename State, typename Start>
-__device__ __forceinline__ void walk_bits_start(uint64_t Ep, State &st, Start start)
-{
-    const uint32_t hi = (uint32_t)(Ep >> 32), lo = (uint32_t)Ep;
-    if (hi != 0) {
-        const int nb = 32 - __clz(hi);
-        const int t = nb < NB ? nb : NB;
-        start(st, hi >> (nb - t));
-        uint32_t h = (nb - t) > 0 ? hi << (32 - (nb - t)) : 0u;
-        for (int i = t; i < nb; ++i) {
-            st.step(h >> 31);
-            h <<= 1;
-        }
-#pragma unroll
-        for (int i = 31; i >= 0; --i) st.step((lo >> i) & 1u);
-    } else {
-        const int nb = 32 - __clz(lo);
-        const int t = nb < NB ? nb : NB;
-        start(st, lo >> (nb - t));
-        uint32_t l = (nb - t) > 0 ? lo << (32 - (nb - t)) : 0u;
-        for (int i = t; i < nb; ++i) {
-            st.step(l >> 31);
-            l <<= 1;
-        }
-    }
 }
 
 struct W1MStart {
