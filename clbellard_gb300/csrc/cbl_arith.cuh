@@ -493,12 +493,15 @@ __device__ __forceinline__ uint64_t w2x_pow2(uint64_t E, uint64_t m, uint32_t mp
     return r;
 }
 
-__device__ __forceinline__ uint64_t w2_digits(uint64_t r, uint64_t m, uint32_t mp, uint32_t q[6])
+// N REDC steps down from r < m (two-word m): q[j] are the quotient digits and
+// the result is r 2^(-32 N) mod m.
+template <int N>
+__device__ __forceinline__ uint64_t w2_redc_down(uint64_t r, uint64_t m, uint32_t mp, uint32_t q[N])
 {
     const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
     uint32_t r0 = (uint32_t)r, r1 = (uint32_t)(r >> 32);
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
+    for (int j = 0; j < N; ++j) {
         q[j] = r0 * mp;
         // (r + q m) / 2^32 = hi(q m0 + r) + c 2^32 + q m1 < m, c the carry out
         asm("{\n\t.reg .u32 x, h, c;\n\t"
@@ -511,6 +514,11 @@ __device__ __forceinline__ uint64_t w2_digits(uint64_t r, uint64_t m, uint32_t m
             : "r"(q[j]), "r"(m0), "r"(r0), "r"(r1), "r"(m1));
     }
     return ((uint64_t)r1 << 32) | r0;
+}
+
+__device__ __forceinline__ uint64_t w2_digits(uint64_t r, uint64_t m, uint32_t mp, uint32_t q[6])
+{
+    return w2_redc_down<6>(r, m, mp, q);
 }
 
 // ------------------------------------------------------------ fixed point --

@@ -426,15 +426,24 @@ __global__ void __launch_bounds__(kBlockDD) dd_terms_kernel(double2 *bigsum, uin
         const uint64_t m = (uint64_t)den0 * k + den1;
         if (m == 1) continue;
         const uint32_t mp = neg_inv32((uint32_t)m);
-        const uint64_t E = 10ull * (d - k) + 192ull;
-        uint32_t q[6];
+        // r = 2^(10(d-k)) mod m: the ladder to 2^(10(d-k) + 32 j) and j REDC
+        // steps down (j = 1 one word, 2 two words); no quotient digits.
+        const uint64_t e = 10ull * (d - k);
         uint64_t r;
-        if (m < kW1Max) r = w1_digits(w1_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
-        else if (m < kW1MMax) r = w1_digits(w1m_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
-        else if (m < kW1SMax) r = w1_digits(w1s_pow2(E, (uint32_t)m, mp), (uint32_t)m, mp, q);
-        else if (m < kW2SMax) r = w2_digits(w2s_pow2(E, m, mp), m, mp, q);
-        else if (m < kW2Max) r = w2_digits(w2_pow2(E, m, mp), m, mp, q);
-        else r = w2_digits(w2x_pow2(E, m, mp), m, mp, q);
+        if (m < kW1SMax) {
+            uint32_t y;
+            if (m < kW1Max) y = w1_pow2(e + 32, (uint32_t)m, mp);
+            else if (m < kW1MMax) y = w1m_pow2(e + 32, (uint32_t)m, mp);
+            else y = w1s_pow2(e + 32, (uint32_t)m, mp);
+            r = redc_word(y * mp, (uint32_t)m, y, 0u);
+        } else {
+            uint64_t y;
+            if (m < kW2SMax) y = w2s_pow2(e + 64, m, mp);
+            else if (m < kW2Max) y = w2_pow2(e + 64, m, mp);
+            else y = w2x_pow2(e + 64, m, mp);
+            uint32_t q[2];
+            r = w2_redc_down<2>(y, m, mp, q);
+        }
         // r and m are exact doubles below 2^53; above, exact double-doubles
         DD t = (m < kDDMax) ? dd_div_nn((double)r, (double)m) : dd_div_dd(dd_from_u64(r), dd_from_u64(m));
         if ((k + (uint64_t)sign) & 1ull) { t.hi = -t.hi; t.lo = -t.lo; }
