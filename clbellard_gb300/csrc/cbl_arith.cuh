@@ -521,6 +521,51 @@ __device__ __forceinline__ uint64_t w2_digits(uint64_t r, uint64_t m, uint32_t m
     return w2_redc_down<6>(r, m, mp, q);
 }
 
+// Two ladders at once (terms k and k+32 of one lane): when both exponents have
+// the same bit length (in the same word) the steps interleave, giving the
+// scheduler two independent chains; otherwise they run one after the other.
+template <int NB, typename State, typename Start>
+__device__ __forceinline__ void walk_bits_start_pair(uint64_t EpA, uint64_t EpB, State &A, State &B, Start start)
+{
+    const uint32_t ha = (uint32_t)(EpA >> 32), la = (uint32_t)EpA, hb = (uint32_t)(EpB >> 32), lb = (uint32_t)EpB;
+    const uint32_t wa = ha ? ha : la, wb = hb ? hb : lb;         // word holding the leading bits
+    const int nba = 32 - __clz(wa), nbb = 32 - __clz(wb);
+    if ((ha == 0) != (hb == 0) || nba != nbb || nba < NB) {
+        walk_bits_start<NB>(EpA, A, start);
+        walk_bits_start<NB>(EpB, B, start);
+        return;
+    }
+    start(A, wa >> (nba - NB));
+    start(B, wb >> (nbb - NB));
+    uint32_t ga = (nba - NB) > 0 ? wa << (32 - (nba - NB)) : 0u, gb = (nbb - NB) > 0 ? wb << (32 - (nbb - NB)) : 0u;
+    for (int i = NB; i < nba; ++i) {
+        A.step(ga >> 31);
+        B.step(gb >> 31);
+        ga <<= 1;
+        gb <<= 1;
+    }
+    if (ha != 0) {
+#pragma unroll
+        for (int i = 31; i >= 0; --i) {
+            A.step((la >> i) & 1u);
+            B.step((lb >> i) & 1u);
+        }
+    }
+}
+
+struct W1Start1 {                                        // the single-bit start of the width-1 kind
+    __device__ __forceinline__ void operator()(W1State &st, uint32_t) const { st.y = w1_start(st.m); }
+};
+
+struct W2SStart {
+    __device__ __forceinline__ void operator()(W2SState &st, uint32_t p) const
+    {
+        const uint64_t y = w2s_start(((uint64_t)st.m1 << 32) | st.m0, p);
+        st.y0 = (uint32_t)y;
+        st.y1 = (uint32_t)(y >> 32);
+    }
+};
+
 // ------------------------------------------------------------ fixed point --
 // 192-bit accumulator as six 32-bit digits, digit 0 least significant.
 struct Acc192 {
