@@ -9,6 +9,8 @@ at the position's d (twice), e.g. a range where one residue kind does all
 the work:
 
     python -m clbellard_gb300.profile_case --position 10000000000 --range 0 3000000000 3100000000
+
+--precision 0 runs that range through the 106-bit double-double kernels instead.
 """
 from __future__ import annotations
 
@@ -24,13 +26,14 @@ def main():
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--range", type=int, nargs=3, metavar=("F", "K0", "K1"))
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2])
     args = ap.parse_args()
     if args.range:
         import time
         f, k0, k1 = args.range
         d, _ = C.pos_to_d(args.position)
-        with C.Context(args.device, 1) as ctx:
-            if args.tile:
+        with C.Context(args.device, args.precision) as ctx:
+            if args.tile and args.precision:
                 ctx.set_tuning(args.tile, args.ctas)
             for _ in range(2):
                 ctx.Set0mem()
@@ -38,7 +41,9 @@ def main():
                 ctx.BatchCalc(k0, k1, f, d)
                 ctx.wait()
                 ms = (time.perf_counter() - t0) * 1e3
-            print("%048x %.3f ms (%d terms, wall)" % (ctx.read_partial(), ms, k1 - k0))
+            part = ctx.read_partial()
+            shown = "%048x" % part if args.precision else "%.17g %.17g" % part
+            print("%s %.3f ms (%d terms, wall)" % (shown, ms, k1 - k0))
         return
     with C.Context(args.device, 1) as ctx:
         if args.tile:
