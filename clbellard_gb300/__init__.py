@@ -94,6 +94,7 @@ def load(build_if_missing: bool = True):
         "cbl_prepared_info": ([vp, P64, P64, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
         "cbl_probe_imad": ([vp, c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)], c_int),
         "cbl_set_tuning": ([vp, c_int, c_int], c_int),
+        "cbl_set_slot_preset": ([vp, P64], c_int),
         "cbl_strerror": ([c_int], ctypes.c_char_p),
         "cbl_pos_to_d_p": ([ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64)], c_int),
         "cbl_compute_p": ([vp, ctypes.POINTER(i64), ctypes.c_char_p], c_int),
@@ -319,6 +320,12 @@ class Context:
                                    ctypes.byref(ms)), "autotune")
         self._prepared = n
         return t.value, c.value, ms.value
+
+    def set_slot_preset(self, preset=None):
+        """Test hook: the six digit sums every slot of later prepared passes
+        starts from (None = zero); see cbl_set_slot_preset."""
+        arr = None if preset is None else (ctypes.c_uint64 * 6)(*[int(x) & (2 ** 64 - 1) for x in preset])
+        _check(load().cbl_set_slot_preset(self._h, arr), "cbl_set_slot_preset")
 
     def set_graph(self, enable: bool):
         _check(load().cbl_set_graph(self._h, 1 if enable else 0), "set_graph")

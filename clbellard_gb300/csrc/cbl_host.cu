@@ -18,15 +18,6 @@
 #include <sys/types.h>
 #include <new>
 
-// Every int-returning entry point runs inside this guard, so no C++ exception
-// crosses the C ABI: a failed host allocation returns CBL_E_NOMEM, anything
-// else CBL_E_ARG.
-#define CBL_GUARD_BEGIN try {
-#define CBL_GUARD_END                                                                   \
-    }                                                                                   \
-    catch (const std::bad_alloc &) { return CBL_E_NOMEM; }                              \
-    catch (...) { return CBL_E_ARG; }
-
 
 using namespace cbl;
 
@@ -69,6 +60,8 @@ struct cbl_ctx {
     int prep_nseg = 0;
     uint64_t prep_ntiles = 0;
     uint64_t prep_terms = 0;
+    bool prep_carry = false;                         // a prepared slot may take >= 2^31 flushes
+    uint64_t slot0_tiles = 0;                        // tiles added into slot 0 since it was zeroed
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;   // around the term kernel of the last prepared run
     bool ev_valid = false;
     cudaGraphExec_t graph = nullptr;                 // captured prepared pass
@@ -83,6 +76,8 @@ struct cbl_ctx {
     double2 *d_ddans = nullptr;
     // scratch host
     uint64_t *h_small = nullptr;              // pinned, 8 words
+    // test hook: initial digit sums of the prepared passes' slots (null = zero)
+    unsigned long long *d_preset = nullptr;
 };
 
 extern "C" {
@@ -245,8 +240,11 @@ int run_segments(cbl_ctx *c, std::vector<Seg> &v)
     std::memcpy(c->h_segs, v.data(), sizeof(Seg) * v.size());
     CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(Seg) * v.size(), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), c->st));
+    // slot 0 collects every launch since cbl_Set0mem: carry once it may have
+    // taken 2^31 flushes (at most one per tile)
+    c->slot0_tiles = std::min<uint64_t>(c->slot0_tiles + ntiles, kCarryTiles);
     CK(launch_terms192(c->d_segs, (int)v.size(), ntiles, (uint32_t)c->tile_k, c->d_counter, c->d_slots,
-                       grid_192(c), 256, c->st));
+                       grid_192(c), 256, c->st, 0, slot_needs_carry(c->slot0_tiles)));
     c->launches++;
     return CBL_OK;
 }
@@ -451,6 +449,7 @@ int cbl_destroy(cbl_ctx *c)
     cudaFree(c->d_ddpartial);
     cudaFree(c->d_ddans);
     cudaFreeHost(c->h_small);
+    cudaFree(c->d_preset);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->ev_k0) cudaEventDestroy(c->ev_k0);
     if (c->ev_k1) cudaEventDestroy(c->ev_k1);
@@ -490,6 +489,27 @@ int cbl_set_tuning(cbl_ctx *c, int tile_terms, int ctas_per_sm)
     CBL_GUARD_END
 }
 
+int cbl_set_slot_preset(cbl_ctx *c, const uint64_t preset[6])
+{
+    CBL_GUARD_BEGIN
+    if (!c) return CBL_E_ARG;
+    cudaSetDevice(c->device);
+    CK(cudaStreamSynchronize(c->st));
+    if (!preset) {
+        cudaFree(c->d_preset);
+        c->d_preset = nullptr;
+    } else {
+        if (!c->d_preset && cudaMalloc(&c->d_preset, sizeof(unsigned long long) * 6) != cudaSuccess) {
+            c->d_preset = nullptr;
+            return CBL_E_NOMEM;
+        }
+        CK(cudaMemcpy(c->d_preset, preset, sizeof(unsigned long long) * 6, cudaMemcpyHostToDevice));
+    }
+    drop_graph(c);                                        // the captured pass clears the slots
+    return CBL_OK;
+    CBL_GUARD_END
+}
+
 int cbl_set_graph(cbl_ctx *c, int enable)
 {
     CBL_GUARD_BEGIN
@@ -505,8 +525,12 @@ int cbl_Set0mem(cbl_ctx *c)
     CBL_GUARD_BEGIN
     if (!c) return CBL_E_ARG;
     cudaSetDevice(c->device);
-    if (is192(c)) CK(cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6, c->st));
-    else CK(cudaMemsetAsync(c->d_bigsum, 0, sizeof(double2) * kDDBlocks, c->st));
+    if (is192(c)) {
+        CK(cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6, c->st));
+        c->slot0_tiles = 0;
+    } else {
+        CK(cudaMemsetAsync(c->d_bigsum, 0, sizeof(double2) * kDDBlocks, c->st));
+    }
     return CBL_OK;
     CBL_GUARD_END
 }
@@ -712,6 +736,14 @@ static int upload_prepared(cbl_ctx *c)
     std::vector<Seg> &v = c->prep_segs;
     const int n = c->prep_npos;
     const uint64_t ntiles = order_and_number(v, (uint32_t)c->tile_k);
+    std::vector<uint64_t> slot_tiles((size_t)7 * n, 0);
+    uint64_t max_slot_tiles = 0;
+    for (const Seg &sg : v) {
+        uint64_t &t = slot_tiles[sg.slot];
+        t += (sg.k1 - sg.k0 + c->tile_k - 1) / c->tile_k;
+        max_slot_tiles = std::max(max_slot_tiles, t);
+    }
+    c->prep_carry = slot_needs_carry(max_slot_tiles);
     int rc = ensure_segs(c, (int)v.size());
     if (rc) return rc;
     CK(cudaStreamSynchronize(c->st));
@@ -751,6 +783,20 @@ static int prepare_positions(cbl_ctx *c, const uint64_t *d, const int *shift, in
     return upload_prepared(c);
 }
 
+// A prepared pass carries digit-sum wraps when a slot may take 2^31 or more
+// flushes or starts from a preset.
+static bool prepared_carry(const cbl_ctx *c) { return c->prep_carry || c->d_preset != nullptr; }
+
+// Zero the first nslot slots, or set them to the test preset. Slot 0 is then
+// no longer a known count of flushes from zero for the kernel-by-kernel calls
+// (until cbl_Set0mem).
+static cudaError_t clear_slots(cbl_ctx *c, int nslot)
+{
+    c->slot0_tiles = kCarryTiles;
+    if (c->d_preset) return launch_slot_fill(c->d_slots, nslot, c->d_preset, c->st);
+    return cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6 * nslot, c->st);
+}
+
 // Enqueue the prepared pass: zero slots and tile counter, the persistent term
 // kernel between two events, the combine kernel. The first pass after a
 // prepare is captured into a CUDA graph and every later pass replays it.
@@ -760,11 +806,11 @@ static int enqueue_prepared(cbl_ctx *c, bool capturing)
     // records them when it is replayed; outside a capture that flag is refused
     const unsigned int evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     const int n = c->prep_npos;
-    CK(cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6 * 7 * n, c->st));
+    CK(clear_slots(c, 7 * n));
     CK(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), c->st));
     CK(cudaEventRecordWithFlags(c->ev_k0, c->st, evf));
     CK(launch_terms192(c->d_segs, c->prep_nseg, c->prep_ntiles, (uint32_t)c->tile_k, c->d_counter, c->d_slots,
-                       grid_192(c), 256, c->st));
+                       grid_192(c), 256, c->st, 0, prepared_carry(c)));
     CK(cudaEventRecordWithFlags(c->ev_k1, c->st, evf));
     CK(launch_combine(c->d_slots, n, c->d_shift, c->d_out3, nullptr, c->st));
     return CBL_OK;
@@ -1300,13 +1346,13 @@ int cbl_run_prepared_budget(cbl_ctx *c, double budget_ms, uint64_t *tiles_done, 
     cudaSetDevice(c->device);
     const int n = c->prep_npos;
     if (!c->partial) {                                    // a fresh pass
-        CK(cudaMemsetAsync(c->d_slots, 0, sizeof(unsigned long long) * 6 * 7 * n, c->st));
+        CK(clear_slots(c, 7 * n));
         CK(cudaMemsetAsync(c->d_counter, 0, sizeof(unsigned long long), c->st));
         c->partial = 1;
     }
     const uint64_t budget_ns = (uint64_t)(budget_ms * 1e6) + 1;
     CK(launch_terms192(c->d_segs, c->prep_nseg, c->prep_ntiles, (uint32_t)c->tile_k, c->d_counter, c->d_slots,
-                       grid_192(c), 256, c->st, budget_ns));
+                       grid_192(c), 256, c->st, budget_ns, prepared_carry(c)));
     c->launches++;
     CK(cudaMemcpyAsync(c->h_small, c->d_counter, sizeof(uint64_t), cudaMemcpyDeviceToHost, c->st));
     int rc = sync(c);

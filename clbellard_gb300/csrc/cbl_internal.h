@@ -3,6 +3,16 @@
 #pragma once
 #include <stdint.h>
 #include <cuda_runtime.h>
+#include <new>
+
+// Every int-returning entry point runs inside this guard, so no C++ exception
+// crosses the C ABI: a failed host allocation returns CBL_E_NOMEM, anything
+// else CBL_E_ARG.
+#define CBL_GUARD_BEGIN try {
+#define CBL_GUARD_END                                                                   \
+    }                                                                                   \
+    catch (const std::bad_alloc &) { return CBL_E_NOMEM; }                              \
+    catch (...) { return CBL_E_ARG; }
 
 namespace cbl {
 
@@ -44,14 +54,24 @@ inline uint32_t seg_flags(int sign, int width) { return (uint32_t)(sign & 1) | (
 // Launch wrappers (cbl_kernels.cu).
 // budget_ns = 0: run to the end; else warps stop taking tiles after budget_ns
 // and the finished tiles are [0, *counter).
+// carry: the slots' digit sums may wrap past 2^64 (a slot can receive 2^31 or
+// more flushes since it was zeroed, or it started from a preset); the flushes
+// then carry each wrap into the digit sum two places up (exact mod 2^192).
+// A slot receives at most one flush per tile, so slot_needs_carry() decides it
+// from the tile counts.
 cudaError_t launch_terms192(const Seg *segs, int nseg, uint64_t ntiles, uint32_t tile_k,
                             unsigned long long *counter, unsigned long long *slots, int grid, int block,
-                            cudaStream_t st, uint64_t budget_ns = 0);
+                            cudaStream_t st, uint64_t budget_ns, bool carry);
+constexpr uint64_t kCarryTiles = 1ull << 31;
+inline bool slot_needs_carry(uint64_t max_tiles_per_slot) { return max_tiles_per_slot >= kCarryTiles; }
 // slots (nslot x 6 digit sums) of position i, series f = slots[(slot_base[i] + f) * 6 ..]:
 // out3[3i..3i+2] (word 0 most significant) = sum_f (S_f << (numer_log2[f] + shift[i])).
 // If partial7 != nullptr it also receives the 7 weighted partials per position.
 cudaError_t launch_combine(const unsigned long long *slots, int npos, const int *shift,
                            uint64_t *out3, uint64_t *partial7, cudaStream_t st);
+// slots[0 .. 6*nslot) <- preset[j % 6] (device array of 6), instead of zero.
+cudaError_t launch_slot_fill(unsigned long long *slots, int nslot, const unsigned long long *preset,
+                             cudaStream_t st);
 // Reference-style single-series pieces on 192-bit buffers:
 //  normalise slot 0 into partial[3] (Ssum_192)
 cudaError_t launch_ssum192(const unsigned long long *slots, uint64_t *partial, cudaStream_t st);
@@ -70,7 +90,7 @@ cudaError_t launch_dd_ssum(const double2 *bigsum, int nblk, double2 *partial, cu
 cudaError_t launch_dd_sum7(double2 *partial, double2 *ans, int numer, cudaStream_t st);
 
 // Throughput probe: grid x block threads each run `iters` rounds of 16
-// independent mul.lo.u32 / mul.hi.u32 chains; *ops = multiply halves issued.
+// independent dependent mad.lo.u32 chains; *ops = multiply halves issued.
 cudaError_t launch_probe_imad(uint32_t *sink, int grid, int block, int iters, uint64_t *ops, cudaStream_t st);
 int probe_imad_grid(int sm_count);   // one full wave of probe CTAs
 

@@ -147,9 +147,30 @@ __device__ __forceinline__ void run_tile(const Seg &s, uint64_t kb, uint64_t ke,
     }
 }
 
+// Add v to element j of a slot (six 64-bit digit sums, element j weighing
+// 2^(32j)), exactly mod 2^192 however many tiles land in the slot. An add that
+// wraps element j past 2^64 drops 2^64 * 2^(32j) = one unit of element j+2, so
+// that unit is added there (and again on the rare wrap of that add); from
+// element 6 on the weight is >= 2^192 and vanishes. Each wrap is seen by
+// exactly the atomic that crossed 2^64, so concurrent flushes stay exact.
+__device__ __forceinline__ void slot_add(unsigned long long *slot6, int j, unsigned long long v)
+{
+    for (;;) {
+        const unsigned long long old = atomicAdd(slot6 + j, v);
+        if (old + v >= old) return;
+        j += 2;
+        v = 1ull;
+        if (j >= 6) return;
+    }
+}
+
 // Warp sum of the lanes' 192-bit values, normalised, added into a slot's six
-// 64-bit digit sums (each add < 2^32, so a slot absorbs 2^32 tiles).
-__device__ __forceinline__ void warp_flush(const Acc192 &acc, int lane, unsigned long long *slot6)
+// 64-bit digit sums. Each add is < 2^32, so a slot that receives fewer than
+// 2^32 flushes from zero cannot wrap and takes plain fire-and-forget adds;
+// with carry set (a slot that may receive 2^31 or more flushes, or a preset
+// start value) slot_add carries the wraps, and the number of flushes per slot
+// is unbounded.
+__device__ __forceinline__ void warp_flush(const Acc192 &acc, int lane, unsigned long long *slot6, int carry)
 {
     uint64_t S[6];
 #pragma unroll
@@ -165,7 +186,10 @@ __device__ __forceinline__ void warp_flush(const Acc192 &acc, int lane, unsigned
             const uint64_t t = S[j] + c;
             const uint32_t dj = (uint32_t)t;
             c = t >> 32;
-            if (dj) atomicAdd(slot6 + j, (unsigned long long)dj);
+            if (dj) {
+                if (carry) slot_add(slot6, j, (unsigned long long)dj);
+                else atomicAdd(slot6 + j, (unsigned long long)dj);
+            }
         }
     }
 }
@@ -178,17 +202,36 @@ __device__ __forceinline__ uint64_t global_ns()
 }
 
 // ------------------------------------------------------- terms192 kernel --
+// Fold a warp's accumulated terms of one segment and add them into its slot.
+// Every k of a lane has the parity of seg.k0 + lane (tiles hold an even number
+// of terms), so the lane's sign (-1)^(k + sign) is fixed for the segment.
+__device__ __forceinline__ void flush_segment(const Seg &s, int lane, Acc192 &acc, uint32_t cnt,
+                                              unsigned long long *slots, int carry)
+{
+    if (((s.k0 + (uint64_t)lane + (s.flags & kFlagSign)) & 1ull) != 0) acc_negate_minus(acc, cnt);
+    warp_flush(acc, lane, slots + (size_t)s.slot * 6, carry);
+}
+
 // With budget_ns != 0 a warp takes no new tile once budget_ns have passed
 // since it started. The deadline is checked before the tile counter is
 // incremented, so every tile taken is finished and the finished tiles are
 // exactly [0, counter): a later launch continues from there.
+// A warp keeps its lanes' sums across consecutive tiles of one segment and
+// flushes them when it moves to another segment, when a lane's term count
+// reaches 2^30, and before it exits: one slot update per run of tiles
+// instead of one per tile.
 __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restrict__ segs, int nseg,
                                                              uint64_t ntiles, uint32_t tile_k,
                                                              unsigned long long *counter,
-                                                             unsigned long long *slots, uint64_t budget_ns)
+                                                             unsigned long long *slots, uint64_t budget_ns,
+                                                             int carry)
 {
     const int lane = threadIdx.x & 31;
     const uint64_t t_start = budget_ns ? global_ns() : 0;
+    int cur = -1;                                   // segment of the sums held in acc
+    Acc192 acc;
+    acc_zero(acc);
+    uint32_t cnt = 0;
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) {
@@ -202,14 +245,17 @@ __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restri
             const int mid = (lo + hi + 1) >> 1;
             if (segs[mid].tile0 <= t) lo = mid; else hi = mid - 1;
         }
+        if (lo != cur || __any_sync(0xffffffffu, cnt >= (1u << 30))) {
+            if (cur >= 0) flush_segment(segs[cur], lane, acc, cnt, slots, carry);
+            acc_zero(acc);
+            cnt = 0;
+            cur = lo;
+        }
         const Seg s = segs[lo];
         const uint64_t kb = s.k0 + (t - s.tile0) * tile_k;
         const uint64_t ke = min(s.k1, kb + tile_k);
         const int width = (int)((s.flags >> 4) & 15u);
         const bool tail = kb >= s.d;
-        Acc192 acc;
-        acc_zero(acc);
-        uint32_t cnt = 0;
         if (tail) {
             if (width == 1) run_tile<1, true>(s, kb, ke, lane, acc, cnt);
             else if (width == 5) run_tile<5, true>(s, kb, ke, lane, acc, cnt);
@@ -225,18 +271,17 @@ __global__ void __launch_bounds__(kBlock192) terms192_kernel(const Seg *__restri
             else if (width == 6) run_tile<6, false>(s, kb, ke, lane, acc, cnt);
             else run_tile<2, false>(s, kb, ke, lane, acc, cnt);
         }
-        // Every k of this lane has the parity of kb + lane: sign (-1)^(k + sign).
-        if (((kb + (uint64_t)lane + (s.flags & kFlagSign)) & 1ull) != 0) acc_negate_minus(acc, cnt);
-        warp_flush(acc, lane, slots + (size_t)s.slot * 6);
     }
+    if (cur >= 0) flush_segment(segs[cur], lane, acc, cnt, slots, carry);
 }
 
 cudaError_t launch_terms192(const Seg *segs, int nseg, uint64_t ntiles, uint32_t tile_k,
                             unsigned long long *counter, unsigned long long *slots, int grid, int block,
-                            cudaStream_t st, uint64_t budget_ns)
+                            cudaStream_t st, uint64_t budget_ns, bool carry)
 {
     (void)block;
-    terms192_kernel<<<grid, kBlock192, 0, st>>>(segs, nseg, ntiles, tile_k, counter, slots, budget_ns);
+    terms192_kernel<<<grid, kBlock192, 0, st>>>(segs, nseg, ntiles, tile_k, counter, slots, budget_ns,
+                                                carry ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -290,6 +335,22 @@ __device__ __forceinline__ void add192(uint64_t a[3], const uint64_t b[3])
         a[i] = s + c;
         c = c1 | (a[i] < s);
     }
+}
+
+// Every slot's six digit sums <- preset[0..6) (a test hook: presets near 2^64
+// make the sums wrap within a few tiles).
+__global__ void slot_fill_kernel(unsigned long long *slots, int nslot, const unsigned long long *preset)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nslot * 6) slots[i] = preset[i % 6];
+}
+
+cudaError_t launch_slot_fill(unsigned long long *slots, int nslot, const unsigned long long *preset,
+                             cudaStream_t st)
+{
+    const int b = 256;
+    slot_fill_kernel<<<(nslot * 6 + b - 1) / b, b, 0, st>>>(slots, nslot, preset);
+    return cudaGetLastError();
 }
 
 __global__ void combine_kernel(const unsigned long long *slots, int npos, const int *shift, uint64_t *out3,
@@ -592,11 +653,9 @@ cudaError_t launch_dd_sum7(double2 *partial, double2 *ans, int numer, cudaStream
 namespace cbl {
 
 // ------------------------------------------------------------ IMAD probe --
-// 16 independent mad.wide.u32 chains per thread: each instruction forms both
-// 32-bit halves of a 32x32 product, the most multiply halves per issue this
-// GPU offers (mad.lo.u32 issues at the same rate with one half, mad.hi.u32 at
-// half that rate). The issue rate x 2 is the peak of the term kernels'
-// algorithmic work unit.
+// 16 independent dependent chains of mad.lo.u32 per thread, one multiply half
+// per instruction: the full issue rate of the FMA-heavy pipe, which is the
+// peak of the term kernels' algorithmic work unit (a multiply half).
 __global__ void __launch_bounds__(256) probe_imad_kernel(uint32_t *sink, int iters)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;

@@ -190,6 +190,14 @@ int64_t cbl_launch_count(const cbl_ctx *ctx);
  * (*best_ms is then -1). Leaves the context prepared for pos. */
 int cbl_autotune(cbl_ctx *ctx, const uint64_t *pos, int n, int force, int *best_tile, int *best_ctas,
                  double *best_ms);
+/* Test hook (no counterpart in the reference): the six digit sums every slot of
+ * later prepared passes (cbl_compute, cbl_batch, cbl_run_prepared) starts from,
+ * instead of zero; NULL restores zero. A slot's value is sum_j preset[j]*2^(32j)
+ * mod 2^192, so each series partial grows by that value and the result by
+ * sum_f (value << log2(numer_f)). Presets near 2^64 make the digit sums wrap
+ * within a few tiles, which exercises the carry that keeps results exact however
+ * many tiles land in one slot (positions beyond 2^32 tiles per series). */
+int cbl_set_slot_preset(cbl_ctx *ctx, const uint64_t preset[6]);
 /* Tuning: terms per warp tile (multiple of 32) and persistent CTAs per SM (0 = auto). */
 int cbl_set_tuning(cbl_ctx *ctx, int tile_terms, int ctas_per_sm);
 const char *cbl_strerror(int code);
@@ -204,19 +212,22 @@ const char *cbl_strerror(int code);
  * device and stream and calls no cudaMalloc, cudaFree or other allocating
  * routine. The caller passes pos[0..n) (host) and d_out3n, a device buffer it
  * owns of 3*n uint64_t; d_out3n[3i..3i+2] receives position i's result (most
- * significant word first), as cbl_batch, once `stream` (a cudaStream_t, 0 for
- * the legacy default stream) reaches that point; the call itself returns
- * without waiting.
+ * significant word first), bit-identical to cbl_batch, once `stream` (a
+ * cudaStream_t, 0 for the legacy default stream) reaches that point. The
+ * positions go to the GPU as a kernel argument and the tile table is built on
+ * the device, so the call makes no host-to-device copy: it enqueues a memset
+ * and three kernels and returns without waiting for them.
  * The kernels' scratch is one static device array of CBL_NOALLOC_SCRATCH_BYTES
- * (about 106 KiB) that every GPU loading this library holds until the process
+ * (about 169 KiB) that every GPU loading this library holds until the process
  * exits. The first call on each device looks up that array's device address
  * (cudaGetSymbolAddress) with the device current; make that first call before
  * any stream capture. All calls on a device share the array and each call
  * clears it before use, so calls whose work overlaps on the GPU (different
  * streams, or several host threads) race and corrupt each other's results:
- * serialise them. n > CBL_NOALLOC_MAX_POSITIONS returns CBL_E_LIMIT. */
+ * serialise them. n > CBL_NOALLOC_MAX_POSITIONS returns CBL_E_LIMIT; positions
+ * are validated as in cbl_compute (CBL_E_POSITION). */
 #define CBL_NOALLOC_MAX_POSITIONS 64
-#define CBL_NOALLOC_SCRATCH_BYTES 108032
+#define CBL_NOALLOC_SCRATCH_BYTES 172544
 int cbl_batch_noalloc(const uint64_t *pos, int n, uint64_t *d_out3n, void *stream);
 
 /* ---- HSP-friendly variants: 64-bit arguments by pointer (HSP passes int64 vars

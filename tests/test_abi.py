@@ -114,3 +114,32 @@ def test_driver_binary_built(cbl):
     assert os.path.exists(build.DRIVER)
     r = subprocess.run([build.DRIVER], capture_output=True, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+def test_noalloc_validates_before_touching_the_device(cbl):
+    """cbl_batch_noalloc checks its arguments on the host first: too many
+    positions is CBL_E_LIMIT and a position outside [5, 999999999999999999] is
+    CBL_E_POSITION; the largest valid position passes validation (the kernels
+    cover moduli up to 2^62) and only then needs the GPU."""
+    import ctypes
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    L = cbl.load()
+    fn = L.cbl_batch_noalloc
+    fn.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    dummy = ctypes.c_void_p(16)                     # never dereferenced: every call fails before any launch
+
+    def call(pos):
+        arr = (ctypes.c_uint64 * len(pos))(*pos)
+        return fn(arr, len(pos), dummy, None)
+
+    assert call([10 ** 4] * 65) == -11
+    assert call([4]) == -2
+    assert call([10 ** 18]) == -2
+    assert call([999999999999999999]) in (-3, -5)   # no device / CUDA error, not a position error
+    assert fn(None, 0, None, None) == 0

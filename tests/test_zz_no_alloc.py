@@ -7,8 +7,11 @@ previous call's contents. This file is collected last so that a run stopping
 at the first failure has already run every other test.
 """
 import ctypes
+import time
 
 import pytest
+
+from conftest import load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -67,3 +70,28 @@ def test_noalloc_limit_and_arguments(cbl):
     stream.synchronize()
     with cbl.Context(0, 1) as ctx:
         assert _results(out, MAX_POSITIONS) == ctx.batch(full)
+
+
+def test_noalloc_two_word_moduli_and_asynchronous_return(cbl):
+    """Position 1e10 runs moduli up to 4e10 (> 2^32, the two-word residue
+    kinds). The call only enqueues work: it returns while the GPU is still
+    busy (about a second of work), and the result then equals cbl_batch and
+    the oracle, on two calls in a row."""
+    import torch
+    fn = _noalloc_fn(cbl)
+    want = int(load_golden("oracle_big.json")["10000000000"]["hex192"], 16)
+    with cbl.Context(0, 1) as ctx:
+        assert ctx.batch([10 ** 10]) == [want]
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    out = torch.full((3 * MAX_POSITIONS,), -1, dtype=torch.int64, device="cuda")
+    for _ in range(2):
+        out.fill_(-1)
+        stream.synchronize()
+        t0 = time.perf_counter()
+        assert _call(fn, [10 ** 10, 10 ** 6], out, stream) == 0
+        host_s = time.perf_counter() - t0
+        still_running = not stream.query()
+        stream.synchronize()
+        assert _results(out, 2) == [want, int(load_golden("oracle_small.json")["1000000"]["hex192"], 16)]
+        assert host_s < 0.1 and still_running
