@@ -3,11 +3,17 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 A step is one full pass of the hot path for one position: all 7 series, k in
-[0, d) plus the 20-term tails, summed into the 192-bit result (one persistent
-term kernel + one combine kernel). value = 7*d terms (tails excluded) per
-second of device time, summed over ranks (weak scaling: rank r computes
-position 1e10 + 10r). The reference arm (--impl reference) times the
-reference's CPU implementation of the same path on the host cores.
+[0, d) plus the 20-term tails, summed into the 192-bit result. On one GPU that
+is one persistent term kernel + one combine kernel; on N > 1 GPUs (torchrun)
+the position is split into 8N balanced work-mode jobs (cbl_plan_jobs), each
+rank runs its share, and the 48-hex job partials are merged by an exact
+integer add (workmodeSum), so the metric is time to the position on N GPUs.
+value = 7*d terms (tails excluded) per second of device time. The default
+N = 1 line also reports the batched-positions workload (4096 positions,
+one persistent launch), the 1e11 position with checkpointed passes and its
+P-8 overlap, and the digits the 106-bit double-double mode keeps. The
+reference arm (--impl reference) times the reference's CPU implementation of
+the same path on the host cores.
 """
 from __future__ import annotations
 
@@ -114,7 +120,9 @@ class ClockSampler:
 def cpu_sample_rate(needD: int, target_s: float, threads: int = 0):
     """The oracle (CPU restatement of the reference's path) on a bounded,
     stratified sample of the workload: per series, 16 chunks spread evenly
-    over k in [0, d). Returns (terms/s, sample description, cores)."""
+    over k in [0, d). The chunk length is sized from a probe that runs at
+    least 0.5 s, so the sample itself takes about target_s. Returns (terms/s,
+    sample description, cores, seconds timed, terms timed)."""
     from oracle import oracle as O
     O.build()
     d, _ = O.pos_to_d(needD)
@@ -130,11 +138,17 @@ def cpu_sample_rate(needD: int, target_s: float, threads: int = 0):
                 n += min(d, k0 + L) - k0
         return n, time.perf_counter() - t0
 
-    n, t = run(256)
+    L = 4096
+    while True:
+        n, t = run(L)
+        if t >= 0.5 or L >= d:
+            break
+        L = min(d, int(L * max(2.0, 0.6 / max(t, 1e-3))))
     rate = n / max(t, 1e-6)
-    L = max(256, int(rate * target_s / (7 * 16)))
+    L = max(256, min(d, int(rate * target_s / (7 * 16))))
     n, t = run(L)
-    return n / t, "7 series x 16 chunks of %d k spread over [0,d) at position %d (%d terms)" % (L, needD, n), cores
+    return (n / t, "7 series x 16 chunks of %d k spread over [0,d) at position %d (%d terms, %.1f s)"
+            % (L, needD, n, t), cores, t, n)
 
 
 # ----------------------------------------------------------------- arms --
@@ -172,20 +186,29 @@ def max_over_ranks(x: float, world: int) -> float:
     return float(t.item())
 
 
-def reference_sample_rate(needD: int, target_s: float, threads: int):
+def workload_config(d: int) -> dict:
+    """The config both arms print (identical, so the two lines compare)."""
+    return {"workload": "pi hex position 1e10: 7 series x d=%d terms + 20-term tails, 192-bit fixed point" % d,
+            "position": POSITION, "d": d, "mode": "192-bit integer",
+            "inputs": "none: k and m are generated arithmetically; GPU steps flush L2 (256 MiB write) between "
+                      "steps"}
+
+
+def reference_sample(needD: int, L: int, threads: int):
     """The reference's own kernels (oracle/_ref, compiled from its OpenCL
     sources as C++; precision 2, the 192-bit integer mode) on a stratified
-    sample of the workload: per series, 8 k-ranges spread over [0, d)."""
+    sample of the workload: per series, 8 k-ranges of L terms spread over
+    [0, d). Returns (terms/s, seconds, terms, threads)."""
     from oracle.ref_harness import build as R
-    r = R.run(needD, 2, threads=threads, sample=(1 << 19, 8))
-    rate = r["terms_per_s"]
-    L = max(1 << 19, int(rate * target_s / 56))
     r = R.run(needD, 2, threads=threads, sample=(L, 8))
-    return r["terms_per_s"], ("reference kernels (precision 2) on 7 series x 8 chunks of %d k spread over [0,d) "
-                              "at position %d" % (L, needD)), r.get("threads", threads)
+    n = 56 * L
+    return r["terms_per_s"], n / r["terms_per_s"], n, r.get("threads", threads)
 
 
 def reference_arm(args):
+    """Each step times a bounded sample of the 1e10 workload on all host
+    cores; value = terms of the timed samples / their seconds. The full
+    position's time is extrapolated from that rate and labelled so."""
     world, rank, _ = dist_init()
     if rank != 0:
         return 0
@@ -194,25 +217,39 @@ def reference_arm(args):
     from oracle.ref_harness import build as R
     d, _ = O.pos_to_d(POSITION)
     use_ref = R.runnable()
-    rates = []
-    desc = ""
-    cores = threads
+    if use_ref:
+        # size the sample from a probe of at least 0.5 s
+        L = 1 << 16
+        while True:
+            rate, t, n, cores = reference_sample(POSITION, L, threads)
+            if t >= 0.5:
+                break
+            L *= 4
+        L = max(1 << 16, int(rate * args.ref_seconds / 56))
+        desc = ("reference kernels (precision 2) on 7 series x 8 chunks of %d k spread over [0,d) at position %d"
+                % (L, POSITION))
+    step_s, step_terms = [], []
     for i in range(args.warmup + args.steps):
         if use_ref:
-            r, desc, cores = reference_sample_rate(POSITION, args.ref_seconds, threads)
+            rate, t, n, cores = reference_sample(POSITION, L, threads)
         else:
-            r, desc, cores = cpu_sample_rate(POSITION, args.ref_seconds, threads)
+            rate, desc, cores, t, n = cpu_sample_rate(POSITION, args.ref_seconds, threads)
             desc += ("; the reference's OpenCL/HSP host cannot run here and its kernels were not compiled for "
                      "this machine, so its CPU restatement (oracle/, Montgomery + exact long division) is timed")
         if i >= args.warmup:
-            rates.append(r)
-    value = statistics.median(rates)
+            step_s.append(t)
+            step_terms.append(n)
+    timed_s, terms_timed = sum(step_s), sum(step_terms)
+    value = terms_timed / timed_s
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 7 * d / value * 1000.0,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64 int", "data": "synthetic",
-        "config": {"workload": "pi hex position 1e10, 192-bit fixed point, 7 series x d=%d terms" % d,
-                   "position": POSITION, "d": d, "mode": "192-bit"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * timed_s / len(step_s),
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u32/u64 int",
+        "data": "synthetic", "config": workload_config(d),
+        "extrapolated": True, "timed_s": timed_s, "terms_timed": terms_timed,
+        "ms_per_position_extrapolated": 7 * d / value * 1000.0,
+        "step": "one bounded sample of the 1e10 workload (%d terms); the full position (%d terms) is "
+                "extrapolated from the sampled rate" % (terms_timed // len(step_s), 7 * d),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "reference" if use_ref else "port",
                          "sample": desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -221,13 +258,34 @@ def reference_arm(args):
     return 0
 
 
+def golden(name: str) -> dict:
+    """A committed oracle fixture (tests/golden), or {} when absent."""
+    path = os.path.join(ROOT, "tests", "golden", name)
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def agreeing_digits(a: str, b: str) -> int:
+    n = 0
+    for x, y in zip(a, b):
+        if x != y:
+            break
+        n += 1
+    return n
+
+
 def ours_arm(args):
     world, rank, local = dist_init()
+    if world > 1 or args.split:
+        return split_arm(args, world, rank, local)
     import torch
     import clbellard_gb300 as C
     torch.cuda.set_device(local)
     C.load()
-    needD = POSITION + 10 * rank
+    needD = POSITION
     d, _ = C.pos_to_d(needD)
     ctx = C.Context(local, 1)
     if args.tile:
@@ -236,7 +294,6 @@ def ours_arm(args):
     info = ctx.prepared_info()
     stream = torch.cuda.ExternalStream(ctx.stream, device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
-    # warm-up (also checks the result against the published digits)
     for _ in range(args.warmup):
         ctx.run_prepared()
     ctx.wait()
@@ -246,7 +303,6 @@ def ours_arm(args):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     kern_ms = []
     n0 = ctx.launch_count
-    barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for i in range(args.steps):
@@ -257,12 +313,11 @@ def ours_arm(args):
             ev[i][1].record(stream)
             kern_ms.append(ctx.kernel_ms())
         torch.cuda.synchronize()
-    barrier(world)
     launches = ctx.launch_count - n0
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = max_over_ranks(sum(step_ms) / len(step_ms), world)
+    ms = sum(step_ms) / len(step_ms)
     terms = 7 * d
-    value = terms * world / (ms / 1000.0)
+    value = terms / (ms / 1000.0)
     # end to end through the public call with host buffers (segment table
     # up, 24-byte result down, synchronised), same metric
     e2e_ms = []
@@ -271,7 +326,7 @@ def ours_arm(args):
         t0 = time.perf_counter()
         h = ctx.compute(needD)
         e2e_ms.append((time.perf_counter() - t0) * 1000.0)
-    e2e_ms = max_over_ranks(sum(e2e_ms) / len(e2e_ms), world)
+    e2e_ms = sum(e2e_ms) / len(e2e_ms)
     kms = sum(kern_ms) / len(kern_ms)
     mults = algorithmic_mults(d)
     achieved = mults / (kms / 1000.0) / 1e9
@@ -282,15 +337,15 @@ def ours_arm(args):
             traffic = json.load(open(tp)).get("bytes_per_launch")
         except (OSError, ValueError):
             traffic = None
+    exact = golden("oracle_big.json").get(str(needD), {})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "u32 int (192-bit fixed point)", "data": "synthetic",
-        "config": {"workload": "pi hex position 1e10, 192-bit fixed point, 7 series x d=%d terms + 20-term tails"
-                               % d, "position": needD, "d": d, "mode": "192-bit integer",
-                   "l2": "flushed between steps (256 MiB write); the path reads no HBM inputs",
-                   "tile_terms": args.tile or 2048, "grid": info["grid"], "tiles": info["tiles"]},
-        "e2e": {"value": terms * world / (e2e_ms / 1000.0), "unit": UNIT,
+        "config": workload_config(d),
+        "launch": {"tile_terms": args.tile or 2048, "grid": info["grid"], "tiles": info["tiles"],
+                   "segments": info["segments"]},
+        "e2e": {"value": terms / (e2e_ms / 1000.0), "unit": UNIT,
                 "h2d_bytes_per_step": 48 * info["segments"] + 4, "d2h_bytes_per_step": 24},
         "roofline": {"bound": "int", "achieved": achieved, "peak": peak_ops / 1e9, "unit": "Gmul/s",
                      "frac": achieved / (peak_ops / 1e9), "traffic": traffic,
@@ -300,19 +355,113 @@ def ours_arm(args):
                                     "GPU (no integer peak in MEASURED_PEAKS.json)"},
         "gpu_launches": launches,
         "result_hex": result,
+        "result_equals_oracle": (result == exact["hex192"]) if exact else None,
         "clocks": clk.summary(),
     }
+    pipe = issue_fraction(kms)
+    if pipe:
+        line["roofline"]["pipe"] = pipe
     if h != result:
         line["error"] = "e2e result differs from device-timed result"
-    if rank == 0 and not args.no_cpu_baseline:
-        r, desc, cores = cpu_sample_rate(needD, args.cpu_seconds)
+    if not args.no_cpu_baseline:
+        r, desc, cores, _, _ = cpu_sample_rate(needD, args.cpu_seconds)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
-    if rank == 0 and args.dd:
+    if args.dd:
         line["dd_compare"] = dd_compare(C, local, needD, d)
+        line["dd_digits_kept"] = dd_digits(C, local, needD, result, exact)
+    ctx.close()
+    if args.extras:
+        line["batch"] = batch_report(C, local, args)
+        line["large"] = large_report(C, local, args)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def issue_fraction(kernel_ms: float):
+    """FMA-heavy pipe issue of the term kernel at 1e10, from a committed ncu
+    count (profiles/terms192_issue.json: warp instructions per launch on that
+    pipe and its peak of one warp instruction per 2 cycles per SM
+    sub-partition), against this run's kernel time at the profile's clock."""
+    path = os.path.join(ROOT, "profiles", "terms192_issue.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+    except (OSError, ValueError):
+        return None
+    peak = p["sms"] * p["smsp_per_sm"] * p["warp_inst_per_cycle_per_smsp"] * p["sm_mhz"] * 1e6
+    rate = p["fmaheavy_warp_inst_per_launch"] / (kernel_ms / 1000.0)
+    return {"fmaheavy_warp_inst_per_launch": p["fmaheavy_warp_inst_per_launch"],
+            "fmaheavy_issue_frac": rate / peak, "source": p.get("source", path)}
+
+
+def split_arm(args, world, rank, local):
+    """One position sharded over ranks: 8 balanced jobs per rank
+    (cbl_plan_jobs), each run through cbl_run_job_range, merged with the
+    exact 48-hex add (workmode.distributed_sum) -- the reference's work mode
+    (Bellard_192.hsp:298-340, workmodeSum0_6.hsp:10-31) done in-process."""
+    import torch
+    import clbellard_gb300 as C
+    from clbellard_gb300 import workmode
+    torch.cuda.set_device(local)
+    C.load()
+    needD = POSITION
+    d, _ = C.pos_to_d(needD)
+    ctx = C.Context(local, 1)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+    run = lambda s, k0, k1: ctx.run_job_range(needD, s, k0, k1)   # noqa: E731
+    for _ in range(args.warmup):
+        split_position(needD, world, rank, run)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    wall = []
+    n0 = ctx.launch_count
+    merged = None
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            barrier(world)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ev[i][0].record(stream)
+            mine = split_position(needD, world, rank, run, merge=False)
+            ev[i][1].record(stream)
+            torch.cuda.synchronize()
+            merged = workmode.distributed_sum(mine) if world > 1 else C.workmode_sum(mine)
+            wall.append(time.perf_counter() - t0)
+    launches = ctx.launch_count - n0
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / args.steps, world)
+    e2e_s = max_over_ranks(sum(wall) / len(wall), world)
+    exact = golden("oracle_big.json").get(str(needD), {})
+    line = {
+        "metric": METRIC, "value": 7 * d / (ms / 1000.0), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+        "vs_baseline": None, "dtype": "u32 int (192-bit fixed point)", "data": "synthetic",
+        "config": workload_config(d),
+        "launch": {"split": "%d balanced jobs (cbl_plan_jobs), %d per rank, merged by an exact 48-hex add"
+                            % (8 * world, 8)},
+        "e2e": {"value": 7 * d / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 24 * 8, "note": "host wall time including the job partials' merge"},
+        "gpu_launches": launches,
+        "result_hex": merged,
+        "result_equals_oracle": (merged == exact["hex192"]) if exact else None,
+        "clocks": clk.summary(),
+    }
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
     return 0
+
+
+def split_position(needD, world, rank, run_range, merge=True, jobs_per_rank=8):
+    """This rank's share of the balanced plan for needD: run_range(s, k0, k1)
+    gives each job's 48-hex partial. With merge, all ranks' partials are
+    summed (workmode.distributed_sum when world > 1) and the merged hex is
+    returned; otherwise this rank's partials."""
+    import clbellard_gb300 as C
+    from clbellard_gb300 import workmode
+    jobs = C.plan_jobs(needD, max(7, jobs_per_rank * world))
+    mine = [run_range(s, k0, k1) for s, k0, k1 in workmode.shard(jobs, rank, world)]
+    if not merge:
+        return mine
+    return workmode.distributed_sum(mine) if world > 1 else C.workmode_sum(mine)
 
 
 def batch_positions(n: int, seed: int = 4096):
@@ -323,62 +472,120 @@ def batch_positions(n: int, seed: int = 4096):
     return [int(x) for x in np.rint(10.0 ** rng.uniform(3.0, 9.0, size=n))]
 
 
-def batch_arm(args):
-    """Batched positions: one persistent pass over all positions (graph
-    replay), autotuned on a subsample; reported against the single-position
-    rate at 1e9 with the same tuning."""
+def batch_report(C, device, args, steps=2, warmup=1, tune_n=64):
+    """Batched positions (4096 log-uniform in [1e3, 1e9]) in one persistent
+    pass (graph replay), autotuned on a subsample, against the single-position
+    rate at 1e9 with the same tuning; every position <= 1e5 is checked against
+    the oracle and the 8 largest against single-position compute."""
     import torch
-    import clbellard_gb300 as C
-    torch.cuda.set_device(0)
     pos = batch_positions(args.npos)
     ds = [C.pos_to_d(p)[0] for p in pos]
     terms = 7 * sum(ds)
-    ctx = C.Context(0, 1)
-    tile, ctas, tune_ms = ctx.autotune(pos[:256], force=True)
+    ctx = C.Context(device, 1)
+    tile, ctas, tune_ms = ctx.autotune(pos[:tune_n], force=True)
     ctx.prepare(pos)
     info = ctx.prepared_info()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ctx.run_prepared()
     ctx.wait()
     ms = []
     n0 = ctx.launch_count
-    with ClockSampler(0) as clk:
-        for _ in range(args.steps):
+    with ClockSampler(device) as clk:
+        for _ in range(steps):
             ctx.run_prepared()
             ms.append(ctx.kernel_ms())
     launches = ctx.launch_count - n0
     res = ctx.read_results()
     kms = sum(ms) / len(ms)
-    # single position at the top of the range, same tuning
     ctx.prepare([10 ** 9])
     ctx.run_prepared()
     ctx.run_prepared()
     single_ms = ctx.kernel_ms()
     single_rate = 7 * C.pos_to_d(10 ** 9)[0] / (single_ms / 1000.0)
-    # end to end: the public batch call with host arrays
     t0 = time.perf_counter()
     res2 = ctx.batch(pos)
     e2e_s = time.perf_counter() - t0
-    value = terms / (kms / 1000.0)
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": kms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u32 int (192-bit fixed point)", "data": "synthetic",
-        "config": {"workload": "%d positions log-uniform in [1e3, 1e9] (numpy default_rng(4096)), 192-bit, one "
-                               "persistent launch per pass (CUDA graph replay)" % args.npos,
-                   "positions": args.npos, "terms": terms, "segments": info["segments"], "tiles": info["tiles"],
-                   "tile_terms": tile, "ctas_per_sm": ctas, "autotune_sample_ms": tune_ms},
-        "single_position_1e9_terms_per_s": single_rate,
-        "sweep_over_single": value / single_rate,
-        "e2e": {"value": terms / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 48 * info["segments"] + 4 * args.npos,
-                "d2h_bytes_per_step": 24 * args.npos},
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
-        "results_consistent": res == res2,
-    }
-    print(json.dumps(line), flush=True)
+    # parity of a seeded subset
+    from oracle import oracle as O
+    small = [i for i, p in enumerate(pos) if p <= 10 ** 5]
+    oracle_ok = all(res[i] == O.result(ds[i], 0, 3) for i in small)
+    largest = sorted(range(len(pos)), key=lambda i: -pos[i])[:8]
+    single_ok = all("%048x" % res[i] == ctx.compute(pos[i]) for i in largest)
     ctx.close()
-    return 0
+    torch.cuda.synchronize()
+    value = terms / (kms / 1000.0)
+    return {"value": value, "unit": UNIT, "ms_per_pass": kms, "steps": steps, "warmup": warmup,
+            "workload": "%d positions log-uniform in [1e3, 1e9] (numpy default_rng(4096)), 192-bit, one "
+                        "persistent launch per pass (CUDA graph replay)" % args.npos,
+            "terms": terms, "segments": info["segments"], "tiles": info["tiles"], "tile_terms": tile,
+            "ctas_per_sm": ctas, "autotune": "forced sweep on the first %d positions (%.1f ms best)"
+                                              % (tune_n, tune_ms),
+            "single_position_1e9_terms_per_s": single_rate, "sweep_over_single": value / single_rate,
+            "e2e": {"value": terms / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 48 * info["segments"] + 4 * len(pos),
+                    "d2h_bytes_per_step": 24 * len(pos)},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "results_consistent": res == res2,
+            "checked": {"positions_le_1e5_vs_oracle": len(small), "oracle_ok": oracle_ok,
+                        "largest_8_vs_single_compute": single_ok}}
+
+
+def large_report(C, device, args, needD=10 ** 11):
+    """Position 1e11 in 192-bit mode, run as time-budgeted passes with a
+    checkpoint saved and restored between them; hex position P-8 overlap;
+    the 106-bit double-double mode at the same position and the digits it
+    keeps against the 192-bit result (and the exact value when committed)."""
+    import torch
+    d, _ = C.pos_to_d(needD)
+    out = {"position": needD, "d": d}
+    with C.Context(device, 1) as ctx:
+        ctx.prepare([needD])
+        t0 = time.perf_counter()
+        passes, done, total = 0, 0, 1
+        while done < total:
+            done, total = ctx.run_prepared_budget(args.large_slice_ms)
+            passes += 1
+            if done < total:
+                blob = ctx.checkpoint()
+                ctx.restore(blob)
+        h192 = "%048x" % ctx.read_results()[0]
+        out["ms_192"] = (time.perf_counter() - t0) * 1000.0
+        out["budgeted_passes"] = passes
+        out["terms_per_s_192"] = 7 * d / (out["ms_192"] / 1000.0)
+        out["hex192"] = h192
+        exact = golden("oracle_big.json").get(str(needD), {})
+        if exact:
+            out["equals_oracle_192"] = h192 == exact["hex192"]
+            out["digits_vs_exact_256"] = agreeing_digits(h192, exact["hex256"])
+        # the result's first digit is hex position (10d + 6)/4 + 1; the value
+        # at hex position P - 8 must repeat it from its ninth digit on
+        p = (10 * d + 6) // 4 + 1
+        hm8 = ctx.compute_hexpos(p - 8)
+        out["hexpos"] = p
+        out["overlap_digits_p_minus_8"] = agreeing_digits(hm8[8:], h192)
+    with C.Context(device, 0) as ctxdd:
+        t0 = time.perf_counter()
+        hdd = ctxdd.compute(needD)
+        out["ms_dd"] = (time.perf_counter() - t0) * 1000.0
+        out["hex_dd"] = hdd
+        out["dd_digits_vs_192"] = agreeing_digits(hdd, h192)
+        if exact:
+            out["dd_digits_vs_exact_256"] = agreeing_digits(hdd, exact["hex256"])
+    torch.cuda.synchronize()
+    return out
+
+
+def dd_digits(C, device, needD, h192, exact):
+    """The 106-bit double-double mode at the same position: hex digits that
+    agree with the 192-bit result and with the exact 256-bit value."""
+    with C.Context(device, 0) as ctxdd:
+        t0 = time.perf_counter()
+        hdd = ctxdd.compute(needD)
+        ms = (time.perf_counter() - t0) * 1000.0
+    r = {"position": needD, "hex_dd": hdd, "ms_dd": ms, "digits_vs_192": agreeing_digits(hdd, h192)}
+    if exact:
+        r["digits_vs_exact_256"] = agreeing_digits(hdd, exact["hex256"])
+        r["digits_192_vs_exact_256"] = agreeing_digits(h192, exact["hex256"])
+    return r
 
 
 def dd_compare(C, device, needD, d):
@@ -409,6 +616,22 @@ def dd_compare(C, device, needD, d):
     return out
 
 
+def batch_arm(args):
+    """The batched-positions workload alone, as its own line."""
+    import clbellard_gb300 as C
+    import torch
+    torch.cuda.set_device(0)
+    C.load()
+    r = batch_report(C, 0, args, steps=args.steps, warmup=args.warmup, tune_n=256)
+    line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_pass"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 int (192-bit fixed point)", "data": "synthetic",
+            "config": {"workload": r["workload"]}, "e2e": r["e2e"], "gpu_launches": r["gpu_launches"],
+            "clocks": r["clocks"], "batch": r}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -422,8 +645,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", default="single", choices=["single", "batch"])
     ap.add_argument("--npos", type=int, default=4096)
+    ap.add_argument("--split", action="store_true", help="shard the position into jobs even on one GPU")
     ap.add_argument("--dd", action="store_true", default=True)
     ap.add_argument("--no-dd", dest="dd", action="store_false")
+    ap.add_argument("--extras", action="store_true", default=True,
+                    help="also report the batched-positions and 1e11 workloads (default)")
+    ap.add_argument("--no-extras", dest="extras", action="store_false")
+    ap.add_argument("--large-slice-ms", type=float, default=3000.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

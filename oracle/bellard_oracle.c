@@ -66,7 +66,9 @@ uint64_t orc_pow2mod(uint64_t e, uint64_t m)
     uint64_t mp = neg_inv64(m);
     uint64_t one = ((uint64_t)0 - m) % m;   /* R mod m: Montgomery form of 1 */
     uint64_t x = one;
-    for (int b = 63; b >= 0; b--) {
+    /* Leading zero bits square the Montgomery one into itself: start at the top set bit. */
+    int top = e ? 63 - __builtin_clzll(e) : -1;
+    for (int b = top; b >= 0; b--) {
         x = redc64((u128)x * x, m, mp);
         if ((e >> b) & 1) { x += x; x = (x >= m) ? x - m : x; }   /* 2x < 2^64 */
     }
@@ -94,7 +96,7 @@ static void frac_words(uint64_t r, uint64_t m, int W, uint64_t *q)
     for (int i = W - 1; i >= 0; i--) {
         u128 num = rem << 64;
         q[i] = (uint64_t)(num / m);
-        rem = num % m;
+        rem = num - (u128)q[i] * m;
     }
 }
 
@@ -180,6 +182,59 @@ void orc_sum_range(uint64_t d, int f, uint64_t k0, uint64_t k1, int W, int nthre
 void orc_series(uint64_t d, int f, int W, int nthreads, uint64_t *out)
 {
     orc_sum_range(d, f, 0, d + (uint64_t)orc_tail_terms(W), W, nthreads, out);
+}
+
+/* The W = 3 and W = 4 sums of one series in one pass. The W = 3 long division
+ * of r*2^192/m yields the first three quotient words of the W = 4 division of
+ * r*2^256/m, so a W = 3 term is the W = 4 term's top three words (also for the
+ * tail: floor(2^(256-10i)/m) >> 64 = floor(2^(192-10i)/m), and the sign fold
+ * acts word by word). The W = 3 sum stops after its 20 tail terms. */
+void orc_sum_range34(uint64_t d, int f, uint64_t k0, uint64_t k1, int nthreads, uint64_t *out3, uint64_t *out4)
+{
+    uint64_t total3[3] = {0}, total4[4] = {0};
+    uint64_t k3end = d + (uint64_t)orc_tail_terms(3);
+    if (k1 > k0) {
+#ifdef _OPENMP
+        int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel num_threads(nt)
+#endif
+        {
+            uint64_t acc3[3] = {0}, acc4[4] = {0}, t[4];
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4096)
+#endif
+            for (long long kk = 0; kk < (long long)(k1 - k0); kk++) {
+                uint64_t k = k0 + (uint64_t)kk;
+                orc_term(d, f, k, 4, t);
+                add_words(acc4, t, 4);
+                if (k < k3end) add_words(acc3, t + 1, 3);
+            }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+            {
+                add_words(total3, acc3, 3);
+                add_words(total4, acc4, 4);
+            }
+        }
+    }
+    (void)nthreads;
+    memcpy(out3, total3, sizeof total3);
+    memcpy(out4, total4, sizeof total4);
+}
+
+void orc_result34(uint64_t d, int shift, int nthreads, uint64_t *out3, uint64_t *out4)
+{
+    uint64_t acc3[3] = {0}, acc4[4] = {0}, s3[3], s4[4];
+    for (int f = 0; f < 7; f++) {
+        orc_sum_range34(d, f, 0, d + (uint64_t)orc_tail_terms(4), nthreads, s3, s4);
+        shl_words(s3, 3, orc_numer_log2[f] + shift);
+        shl_words(s4, 4, orc_numer_log2[f] + shift);
+        add_words(acc3, s3, 3);
+        add_words(acc4, s4, 4);
+    }
+    memcpy(out3, acc3, sizeof acc3);
+    memcpy(out4, acc4, sizeof acc4);
 }
 
 void orc_result(uint64_t d, int shift, int W, int nthreads, uint64_t *out)

@@ -64,6 +64,12 @@ void orc_series(uint64_t d, int f, int W, int nthreads, uint64_t *out);
 /* frac(2^(10d+6+shift) * pi) as W words: sum_f S_f << (numer_log2[f] + shift). */
 void orc_result(uint64_t d, int shift, int W, int nthreads, uint64_t *out);
 
+/* The W = 3 and W = 4 results (and one-series sums over [k0, k1)) from one
+ * pass over k: the W = 3 words equal orc_result(.., 3, ..) and the W = 4 words
+ * orc_result(.., 4, ..). */
+void orc_sum_range34(uint64_t d, int f, uint64_t k0, uint64_t k1, int nthreads, uint64_t *out3, uint64_t *out4);
+void orc_result34(uint64_t d, int shift, int nthreads, uint64_t *out3, uint64_t *out4);
+
 /* General hex position p >= 3 (1-based digit after the point): d and shift with
  * 4(p-1) = 10d + 6 + shift, 0 <= shift < 10. Returns -1 if p < 3. */
 int orc_hexpos_to_d(uint64_t p, uint64_t *d, int *shift);

@@ -50,6 +50,8 @@ def lib():
         L.orc_sum_range.argtypes = [u64, ctypes.c_int, u64, u64, ctypes.c_int, ctypes.c_int, P64]
         L.orc_series.argtypes = [u64, ctypes.c_int, ctypes.c_int, ctypes.c_int, P64]
         L.orc_result.argtypes = [u64, ctypes.c_int, ctypes.c_int, ctypes.c_int, P64]
+        L.orc_sum_range34.argtypes = [u64, ctypes.c_int, u64, u64, ctypes.c_int, P64, P64]
+        L.orc_result34.argtypes = [u64, ctypes.c_int, ctypes.c_int, P64, P64]
         L.orc_tail_terms.argtypes = [ctypes.c_int]
         L.orc_to_hex.argtypes = [P64, ctypes.c_int, ctypes.c_char_p]
         L.orc_hex48_sum.argtypes = [ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.c_char_p]
@@ -113,6 +115,20 @@ def result(d: int, shift: int = 0, W: int = 3, nthreads: int = 0) -> int:
     out = (ctypes.c_uint64 * W)()
     lib().orc_result(d, shift, W, nthreads, out)
     return _words_to_int(out, W)
+
+
+def sum_range34(d: int, f: int, k0: int, k1: int, nthreads: int = 0):
+    """(W=3 sum, W=4 sum) of series f over [k0, k1) from one pass."""
+    o3, o4 = (ctypes.c_uint64 * 3)(), (ctypes.c_uint64 * 4)()
+    lib().orc_sum_range34(d, f, k0, k1, nthreads, o3, o4)
+    return _words_to_int(o3, 3), _words_to_int(o4, 4)
+
+
+def result34(d: int, shift: int = 0, nthreads: int = 0):
+    """(result(d, shift, 3), result(d, shift, 4)) from one pass over k."""
+    o3, o4 = (ctypes.c_uint64 * 3)(), (ctypes.c_uint64 * 4)()
+    lib().orc_result34(d, shift, nthreads, o3, o4)
+    return _words_to_int(o3, 3), _words_to_int(o4, 4)
 
 
 def to_hex(x: int, W: int = 3) -> str:

@@ -24,7 +24,8 @@ ORACLE = os.path.dirname(HERE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
 BINARY = os.path.join(OUT_DIR, "ref_bellard")
 BINARY_OD = os.path.join(OUT_DIR, "ref_bellard_od")
-REFERENCE = "/root/reference"
+# The reference tree is read where it lies; CBL_REFERENCE_DIR overrides the default location.
+REFERENCE = os.environ.get("CBL_REFERENCE_DIR", "/root/reference")
 SOURCES = ("Bellard.cl", "Bellard_div2by1.cl")
 LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
 

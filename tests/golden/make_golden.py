@@ -1,7 +1,7 @@
 """Generate the oracle golden fixtures in tests/golden/.
 
     python tests/golden/make_golden.py            # small positions (seconds)
-    python tests/golden/make_golden.py --big 1000000000 10000000000   # hours of CPU
+    python tests/golden/make_golden.py --big 100000000000   # 1e11: hours on 8 cores
 
 Each fixture records, for a reference position needD, the oracle's 192-bit
 result (the bit-exact definition the CUDA kernels reproduce) and its 256-bit
@@ -29,12 +29,10 @@ SMALL = [5, 10, 15, 100, 1000, 10000, 100000, 1000000, 10000000]
 def entry(needD: int, threads: int) -> dict:
     d, adj = O.pos_to_d(needD)
     t0 = time.time()
-    r3 = O.result(d, 0, 3, threads)
+    r3, r4 = O.result34(d, 0, threads)      # both widths from one pass over k
     t1 = time.time()
-    r4 = O.result(d, 0, 4, threads)
-    t2 = time.time()
     return {"needD": adj, "d": d, "hex192": O.to_hex(r3, 3), "hex256": O.to_hex(r4, 4),
-            "seconds_192": round(t1 - t0, 2), "seconds_256": round(t2 - t1, 2), "threads": threads}
+            "seconds_192_256": round(t1 - t0, 2), "threads": threads or os.cpu_count()}
 
 
 def main():

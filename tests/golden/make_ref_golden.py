@@ -4,9 +4,11 @@ positions in all three precision modes. Needs the reference tree; the
 committed JSON is what the tests read.
 
     python tests/golden/make_ref_golden.py [--big]
+    python tests/golden/make_ref_golden.py --positions 10000000000 --modes 2 1 0
 """
 from __future__ import annotations
 
+import argparse
 import json
 import os
 import sys
@@ -31,21 +33,28 @@ def dd_hex(hi: float, lo: float) -> str:
 
 
 def main():
-    big = "--big" in sys.argv
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--big", action="store_true", help="position 1e8 (minutes)")
+    ap.add_argument("--positions", type=int, nargs="*", default=None,
+                    help="explicit positions (1e10: about 30 min per mode on 8 threads)")
+    ap.add_argument("--modes", type=int, nargs="*", default=[0, 1, 2])
+    args = ap.parse_args()
     path = os.path.join(HERE, "ref_outputs.json")
     data = json.load(open(path)) if os.path.exists(path) else {}
     data["source"] = ("reference kernels Bellard.cl / Bellard_div2by1.cl compiled as C++ (oracle/ref_harness), "
                       "64 work-groups x 256 work-items, launch sequence of KernelFuncs.as")
-    for p in (BIG if big else POSITIONS):
-        e = {}
-        for prec in (0, 1, 2):
-            r = R.run(p, prec)
+    positions = args.positions if args.positions else (BIG if args.big else POSITIONS)
+    for p in positions:
+        for prec in args.modes:
+            r = R.run(p, prec, timeout=6 * 3600.0)
+            data = json.load(open(path)) if os.path.exists(path) else data
+            e = data.setdefault(str(p), {})
             e["d"] = r["d"]
             e["mode%d" % prec] = dd_hex(*r["dd"]) if prec == 0 else r["hex"]
             e["mode%d_seconds" % prec] = r["seconds"]
-        data[str(p)] = e
-        json.dump(data, open(path, "w"), indent=1, sort_keys=True)
-        print(p, e, flush=True)
+            e["threads"] = r.get("threads")
+            json.dump(data, open(path, "w"), indent=1, sort_keys=True)
+            print(p, prec, e, flush=True)
 
 
 if __name__ == "__main__":

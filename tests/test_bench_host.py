@@ -60,3 +60,47 @@ def test_max_over_ranks_gloo():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert got == {0: 11.0, 1: 11.0}
+
+
+def _split_rank(rank, world, port, needD, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank), CUDA_VISIBLE_DEVICES="")
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import oracle as O
+    w, r, _ = bench.dist_init()
+    d, _ = O.pos_to_d(needD)
+
+    def run_range(s, k0, k1):
+        # the oracle's partial of job (s, [k0, k1)): what cbl_run_job_range returns
+        return "%048x" % ((O.sum_range(d, s, k0, k1, 3) << O.NUMER_LOG2[s]) % (1 << 192))
+
+    try:
+        q.put((r, bench.split_position(needD, w, r, run_range)))
+    finally:
+        if w > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+def test_split_position_two_gloo_ranks_gives_single_rank_bits(oracle):
+    """bench.py's multi-GPU path: one position cut into 8 balanced jobs per
+    rank, each rank runs its share, and the exact 48-hex merge over the ranks
+    equals the position's result (here with the oracle standing in for the
+    GPU job)."""
+    import multiprocessing as mp
+    needD = 123455
+    d, _ = oracle.pos_to_d(needD)
+    want = oracle.to_hex(oracle.result(d, 0, 3), 3)
+    ctx = mp.get_context("spawn")
+    for world in (1, 2):
+        q = ctx.Queue()
+        port = _free_port()
+        procs = [ctx.Process(target=_split_rank, args=(r, world, port, needD, q)) for r in range(world)]
+        for p in procs:
+            p.start()
+        got = dict(q.get(timeout=180) for _ in procs)
+        for p in procs:
+            p.join(timeout=60)
+            assert p.exitcode == 0
+        assert set(got.values()) == {want}, (world, got)
