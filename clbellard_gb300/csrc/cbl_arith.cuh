@@ -18,7 +18,7 @@
 //   width 1 (m < 2^28): R = 2^32, residues kept lazily in [0, 4m).
 //   middle width 1 (2^28 <= m < 2^31): R = 2^32, residues in [0, m).
 //   strict width 1 (2^28 <= m < 2^32): R = 2^32, residues in [0, m), carries kept.
-//   short width 2 (2^32 <= m < 2^44): R = 2^64, residues in [0, 4m).
+//   short width 2 (2^32 <= m < 2^44): R = 2^48, residues in [0, 4m).
 //   width 2 (2^28 <= m < 2^60): R = 2^64 by two word steps, residues in [0, 4m).
 //   wide width 2 (2^60 <= m < 2^62): the same steps with residues in [0, 2m).
 // The ladder step is y <- REDC(y^2) << b with b the next exponent bit; in the
@@ -357,14 +357,17 @@ __device__ __forceinline__ uint64_t w2_pow2(uint64_t E, uint64_t m, uint32_t mp)
 }
 
 // --------------------------------------------------- width 2, m < 2^44 --
-// 2^32 <= m < 2^44 (m1 < 2^12), y in [0,4m) (y1 < 2^14). Same REDC_2^64 as
-// w2_sqr over the short top words: y^2 = y0^2 + y0 (2 y1) 2^32 + y1^2 2^64
-// with y0 (2 y1) < 2^47 and y1^2 < 2^28, so word step 1 is
+// 2^32 <= m < 2^44 (m1 < 2^12), y in [0,4m) (y1 < 2^14), R = 2^48: one 32-bit
+// REDC word step and one 16-bit step. R > 16m^2/(3m) keeps the lazy residues
+// in [0, 4m): REDC(y^2) < 16m^2/2^48 + m < 2m. y^2 = y0^2 + y0 (2 y1) 2^32 +
+// y1^2 2^64 with y0 (2 y1) < 2^47 and y1^2 < 2^28, so word step 1 is
 //   s = (y0^2 + u0 m0) / 2^32 + y1^2 2^32 + y0 (2 y1) + u0 m1 < 2^61,
 // one carry chain whose carry out of the first multiply-add lands on y1^2
-// (its high words stay below 2^29 and 2^30: no carry leaves the chain);
-// word step 2 is z = (s + u1 m0) / 2^32 + u1 m1 < m + 2^29 < 2m with its
-// carry out placed in the high word. (The chain holds up to m < 2^46.)
+// (its high words stay below 2^29 and 2^30: no carry leaves the chain).
+// The 16-bit step takes u1 = s0 mp mod 2^16, so u1 m1 < 2^28 is a single low
+// multiply (a 32-bit step needs two words there): X = s + u1 m0 + u1 m1 2^32
+// < 2^62 with its low 16 bits zero, and X / 2^16 < 2m. The doubling joins
+// that shift: y = X >> (16 - b). 14 multiply halves per step instead of 15.
 __device__ __forceinline__ void w2s_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0, uint32_t m1, uint32_t mp,
                                         uint32_t b)
 {
@@ -384,18 +387,16 @@ __device__ __forceinline__ void w2s_sqr(uint32_t &y0, uint32_t &y1, uint32_t m0,
         "madc.hi.u32 %1, %2, %9, t1;\n\t}"
         : "=r"(s0), "=r"(s1)
         : "r"(u0), "r"(m0), "r"(a0), "r"(a1), "r"(ysq), "r"(y0), "r"(y2), "r"(m1));
-    const uint32_t u1 = s0 * mp;
-    uint32_t z0, z1;
-    asm("{\n\t.reg .u32 x0, yw, c2;\n\t"
-        "mad.lo.cc.u32 x0, %2, %3, %4;\n\t"     // u1 m0 + s: low word 0
-        "madc.hi.cc.u32 yw, %2, %3, %5;\n\t"
-        "addc.u32 c2, 0, 0;\n\t"
-        "mad.lo.cc.u32 %0, %2, %6, yw;\n\t"     // + u1 m1
-        "madc.hi.u32 %1, %2, %6, c2;\n\t}"
-        : "=r"(z0), "=r"(z1)
+    const uint32_t u1 = (s0 * mp) & 0xffffu;
+    uint32_t x0, x1;
+    asm("mad.lo.cc.u32 %0, %2, %3, %4;\n\t"     // u1 m0 + s: low 16 bits 0
+        "madc.hi.u32 %1, %2, %3, %5;\n\t"
+        "mad.lo.u32 %1, %2, %6, %1;"              // + u1 m1 2^32
+        : "=&r"(x0), "=&r"(x1)
         : "r"(u1), "r"(m0), "r"(s0), "r"(s1), "r"(m1));
-    y1 = __funnelshift_l(z0, z1, b);
-    y0 = z0 << b;
+    const uint32_t sh = 16u - b;
+    y0 = __funnelshift_r(x0, x1, sh);
+    y1 = x1 >> sh;
 }
 
 struct W2SState {
@@ -403,35 +404,32 @@ struct W2SState {
     __device__ __forceinline__ void step(uint32_t b) { w2s_sqr(y0, y1, m0, m1, mp, b); }
 };
 
-// A value in (0, 2m) congruent to 2^(64 + p), 1 <= p <= 15, for 2^32 <= m < 2^44:
-// q1 = trunc(2^(64+p) / m) from a float reciprocal leaves |r1| <= 2^(43+p) + m
-// (< 2^59); q2 = rint(r1 / m) (|q2| <= 2^27) is off by a few units, so
-// |r2| <= ~25m; q3 = rint(r2 / m) is then exact to within one half, and
-// r2 + (1 - q3) m lies in (0, 2m). The q2 m product is taken mod 2^64: r2 is
-// small, so the wrapped difference is exact.
+// A value in (0, 2m) congruent to 2^(48 + p), 1 <= p <= 15, for 2^32 <= m < 2^44:
+// q1 = trunc(2^(48+p) / m) from a float reciprocal (q1 < 2^31) leaves
+// |r1| <= 2^(27+p) + m; q2 = rint(r1 / m) (|r1 / m| < 2^11) is then off by at
+// most a few thousandths, so r1 - q2 m lies in (-m/2, m/2) up to that slack and
+// r1 + (1 - q2) m in (0, 2m). (Checked in float32 emulation over 4e5 moduli,
+// every p, with reciprocals off by up to 2 ulps.)
 __device__ __forceinline__ uint64_t w2s_start(uint64_t m, uint32_t p)
 {
     const uint32_t m0 = (uint32_t)m, m1 = (uint32_t)(m >> 32);
     const float fm = __fmaf_rn(__uint2float_rn(m1), 4294967296.0f, __uint2float_rn(m0));
     const float inv = rcp_approx(fm);
-    const float scale = __int_as_float((int)((127u + 64u + p) << 23));      // 2^(64+p)
+    const float scale = __int_as_float((int)((127u + 48u + p) << 23));      // 2^(48+p)
     const uint64_t q1 = float_to_u64_trunc(scale * inv);
-    const int64_t r1 = (int64_t)(0ull - q1 * m);
+    const int64_t r1 = (int64_t)((1ull << (48 + p)) - q1 * m);
     const float fr1 = __fmaf_rn(__int2float_rn((int32_t)(r1 >> 32)), 4294967296.0f,
                                 __uint2float_rn((uint32_t)r1));
     const int32_t q2 = __float2int_rn(fr1 * inv);
-    const int64_t r2 = (int64_t)((uint64_t)r1 - (uint64_t)((int64_t)q2 * (int64_t)m));   // exact mod 2^64
-    const float fr2 = __fmaf_rn(__int2float_rn((int32_t)(r2 >> 32)), 4294967296.0f,
-                                __uint2float_rn((uint32_t)r2));
-    const int32_t q3 = __float2int_rn(fr2 * inv);
-    return (uint64_t)(r2 + (int64_t)(1 - q3) * (int64_t)m);
+    return (uint64_t)(r1 + (int64_t)(1 - q2) * (int64_t)m);
 }
 
-// r6 = 2^E mod m in [0, m) for E >= 65, 2^32 <= m < 2^44. The start value
-// takes the leading up-to-four bits of E - 64 at once.
+// r6 = 2^E mod m in [0, m) for E >= 65, 2^32 <= m < 2^44. The ladder runs in
+// Montgomery form with R = 2^48 on the bits of E - 48; the start value takes
+// their leading up-to-four bits at once.
 __device__ __forceinline__ uint64_t w2s_pow2(uint64_t E, uint64_t m, uint32_t mp)
 {
-    const uint64_t Ep = E - 64;
+    const uint64_t Ep = E - 48;
     const uint32_t hi = (uint32_t)(Ep >> 32), lo = (uint32_t)Ep;
     W2SState st{0, 0, (uint32_t)m, (uint32_t)(m >> 32), mp};
     if (hi != 0) {

@@ -92,7 +92,7 @@ __device__ __forceinline__ void term_pair(uint64_t d, uint64_t ka, uint64_t ma, 
     const uint64_t Ea = 10ull * (d - ka) + 192ull, Eb = Ea - 320ull;
     if (KIND == 4) {
         W2SState A{0, 0, (uint32_t)ma, (uint32_t)(ma >> 32), mpa}, B{0, 0, (uint32_t)mb, (uint32_t)(mb >> 32), mpb};
-        walk_bits_start_pair<4>(Ea - 64, Eb - 64, A, B, W2SStart{});
+        walk_bits_start_pair<4>(Ea - 48, Eb - 48, A, B, W2SStart{});   // R = 2^48
         uint64_t ra = ((uint64_t)A.y1 << 32) | A.y0, rb = ((uint64_t)B.y1 << 32) | B.y0;
         ra = min(ra, ra - 2 * ma);
         ra = min(ra, ra - ma);
