@@ -95,6 +95,7 @@ def load(build_if_missing: bool = True):
         "cbl_probe_imad": ([vp, c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)], c_int),
         "cbl_set_tuning": ([vp, c_int, c_int], c_int),
         "cbl_set_slot_preset": ([vp, P64], c_int),
+        "cbl_hex_dd": ([ctypes.c_double, ctypes.c_double, ctypes.c_char_p], c_int),
         "cbl_strerror": ([c_int], ctypes.c_char_p),
         "cbl_pos_to_d_p": ([ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64)], c_int),
         "cbl_compute_p": ([vp, ctypes.POINTER(i64), ctypes.c_char_p], c_int),
@@ -149,6 +150,13 @@ def plan_jobs(needD: int, njobs: int):
     K1 = (ctypes.c_uint64 * njobs)()
     n = _check(L.cbl_plan_jobs(needD, njobs, S, K0, K1, njobs), "cbl_plan_jobs")
     return [(S[i], K0[i], K1[i]) for i in range(n)]
+
+
+def hex_dd(hi: float, lo: float) -> str:
+    """Mode-0 print form of a double-double (cbl_hex_dd)."""
+    out = ctypes.create_string_buffer(49)
+    _check(load().cbl_hex_dd(hi, lo, out), "cbl_hex_dd")
+    return out.value.decode()
 
 
 def words_to_int(w) -> int:

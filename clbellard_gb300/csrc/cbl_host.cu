@@ -289,11 +289,24 @@ u128 fixed128_abs(double x)
     return (sh > -64) ? (u128)(mi >> (-sh)) : 0;
 }
 
-// Mode-0 hex: the double-double value in [0,1) to 28 hex digits (14 bytes, as
-// hexadecimal_dd, hexsademical.as:21-101) and 20 trailing zeros. The sum is
-// formed mod 2^128, which is exact for a value in [0,1).
+// Mode-0 hex: the double-double value mod 1 to 28 hex digits (14 bytes, as
+// hexadecimal_dd, hexsademical.as:21-101) and 20 trailing zeros. A negative
+// value is first lifted by 1.0 with the reference's own double-double add
+// (hexsademical.as:3-19, 25-31: two-sum, the low words added in order, two-sum),
+// whose rounding of the low word the printed bytes keep; then the sum is formed
+// mod 2^128, exactly, and truncated. The reference's byte loop is exact except
+// for its borrow branch (hexsademical.as:73-97), which leaves every later byte
+// 00; this truncation prints those bytes' true values.
 void dd_to_hex(double hi, double lo, char out[49])
 {
+    if (hi < 0.0) {
+        const double x = hi + 1.0, t = x - hi;
+        double y = (hi - (x - t)) + (1.0 - t);
+        y = y + lo + 0.0;
+        const double x2 = x + y, t2 = x2 - x;
+        lo = (x - (x2 - t2)) + (y - t2);
+        hi = x2;
+    }
     u128 u = hi < 0 ? (u128)0 - fixed128_abs(hi) : fixed128_abs(hi);
     u += lo < 0 ? (u128)0 - fixed128_abs(lo) : fixed128_abs(lo);
     const uint64_t top = (uint64_t)(u >> 64), low = (uint64_t)u;
@@ -355,6 +368,16 @@ const char *cbl_strerror(int code)
     case CBL_E_LIMIT: return "request exceeds a fixed limit (at most CBL_NOALLOC_MAX_POSITIONS positions)";
     default: return "unknown error";
     }
+}
+
+int cbl_hex_dd(double hi, double lo, char hex[49])
+{
+    CBL_GUARD_BEGIN
+    if (!hex || !std::isfinite(hi) || !std::isfinite(lo) || std::fabs(hi) >= 1.0 || std::fabs(lo) >= 1.0)
+        return CBL_E_ARG;
+    dd_to_hex(hi, lo, hex);
+    return CBL_OK;
+    CBL_GUARD_END
 }
 
 int cbl_formula(int f, uint64_t *numer, int64_t *numesign, uint64_t *den0, uint64_t *den1)

@@ -113,6 +113,14 @@ int cbl_compute(cbl_ctx *ctx, uint64_t needD, char hex[49]);
 /* Any hex position p >= 3 (not limited to multiples of 5): frac(16^(p-1) pi).
  * The low `shift` bits (shift = 4(p-1)-6 mod 10 <= 9) of the 192 are zero. */
 int cbl_compute_hexpos(cbl_ctx *ctx, uint64_t p, char hex[49]);
+/* Mode-0 result printer (replaces hexadecimal_dd, hexsademical.as:21-101): a
+ * double-double hi + lo (|hi|, |lo| < 1) taken mod 1, as 28 hex digits (112
+ * bits) and 20 zeros. A negative value is lifted by 1.0 with the reference's
+ * own double-double add, then truncated exactly: the reference's bytes, except
+ * after a negative intermediate byte (hexsademical.as:73-97), where the
+ * reference keeps x + 256 as the remainder and prints every later byte as 00;
+ * here those bytes are the value's own. Host only. */
+int cbl_hex_dd(double hi, double lo, char hex[49]);
 /* Work-mode job (s, b) (*Batchloop body, Bellard_192.hsp:304-333): terms
  * k in [b*batchsize, (b+1)*batchsize) of series s, weighted by numer; hex is
  * line 0 of the reference's work/<s>/<s>_<b>.txt. CBL_SKIPPED if b*batchsize > d. */

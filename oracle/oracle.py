@@ -179,6 +179,117 @@ def py_result(d: int, shift: int = 0, W: int = 3) -> int:
     return acc & mask
 
 
+# ---- the reference's mode-0 printer, restated ------------------------------
+def _twosum(a: float, b: float):
+    """hexsademical.as:3-10."""
+    x = a + b
+    tmp = x - a
+    return x, (a - (x - tmp)) + (b - tmp)
+
+
+def _addcab(a, b):
+    """Double-double add, hexsademical.as:12-19."""
+    x, y = _twosum(a[0], b[0])
+    y = y + a[1] + b[1]
+    return _twosum(x, y)
+
+
+def _hsp_int(x: float) -> int:
+    """HSP int() of a double: truncation toward zero; out of the 32-bit range
+    the x86 conversion yields INT_MIN."""
+    if x != x or not (-2147483649.0 < x < 2147483648.0):
+        return -2147483648
+    return int(x)
+
+
+def hexadecimal_dd(hi: float, lo: float, report: bool = False):
+    """The reference's mode-0 result printer, hexadecimal_dd
+    (hexsademical.as:21-101, printed by hexadecimal_i32 :104-127), restated
+    step by step: a negative value is lifted by 1.0 (:25-31); then 14 times
+    the double-double is scaled by 256 and renormalised (:38-44) and its
+    integer part becomes the next byte, most significant first, into a
+    24-byte little-endian buffer of six 32-bit ints (:46-49). An integer part
+    of exactly 256 writes 0 and carries 1 into the byte before, through the
+    ints (:51-71); a negative remainder writes int(x + 256) and borrows 1 from
+    the byte before (:73-91), then sets the remainder to x + 256 (:92-96), so
+    every later byte reads 00. Bytes 9..0 stay 0: 28 hex digits and 20 zeros.
+    With report=True returns (hex, whether the borrow branch was taken)."""
+    out = bytearray(24)
+    borrowed = False
+
+    def get_int(b):
+        return int.from_bytes(out[4 * b:4 * b + 4], "little", signed=True)
+
+    def set_int(b, v):
+        out[4 * b:4 * b + 4] = (v & 0xffffffff).to_bytes(4, "little")
+
+    def poke(i, v):
+        out[i] = v & 0xff
+
+    if hi < 0.0:
+        hi, lo = _addcab((hi, lo), (1.0, 0.0))
+    for cnt in range(14):
+        hi *= 256.0
+        lo *= 256.0
+        x = hi + lo
+        tmp = x - hi
+        y = (hi - (x - tmp)) + (lo - tmp)
+        hi, lo = x, y
+        moji = _hsp_int(hi)
+        if moji < 256 and hi >= 0.0:
+            poke(23 - cnt, moji)
+            hi -= moji
+            continue
+        if moji == 256:
+            moji = moji % 256
+            idx = 23 - cnt + 1
+            if idx < 24:
+                bidx, lidx = idx // 4, idx % 4
+                addv = 1 << (lidx * 8)
+                set_int(bidx, get_int(bidx) + addv)
+                for _ in range(5 - bidx):
+                    v = get_int(bidx)
+                    if 0 <= v < addv:
+                        bidx += 1
+                        addv = 1
+                        set_int(bidx, get_int(bidx) + addv)
+                    else:
+                        break
+            poke(23 - cnt, moji)
+            hi -= 256.0
+        if hi < 0.0:
+            borrowed = True
+            moji = _hsp_int(hi + 256.0)
+            idx = 23 - cnt + 1
+            if idx < 24:
+                bidx, lidx = idx // 4, idx % 4
+                addv = 1 << (lidx * 8)
+                set_int(bidx, get_int(bidx) - addv)
+                for _ in range(5 - bidx):
+                    v = get_int(bidx)
+                    if -addv <= v < 0:
+                        bidx += 1
+                        addv = 1
+                        set_int(bidx, get_int(bidx) - addv)
+                    else:
+                        break
+            poke(23 - cnt, moji)
+            hi, lo = _addcab((hi, lo), (256.0, 0.0))
+    h = bytes(reversed(out)).hex()
+    return (h, borrowed) if report else h
+
+
+def dd_exact_hex(hi: float, lo: float, lift: bool = False) -> str:
+    """The exact value (hi + lo) mod 1 truncated to 112 bits: 28 hex digits
+    and 20 zeros. With lift, a negative hi is first lifted by 1.0 with the
+    reference's double-double add (hexsademical.as:25-31), rounding included."""
+    from fractions import Fraction
+    if lift and hi < 0.0:
+        hi, lo = _addcab((hi, lo), (1.0, 0.0))
+    v = int((Fraction(hi) + Fraction(lo)) % 1 * (1 << 112))
+    return format(v, "028x") + "0" * 20
+
+
 def agreeing_hex_digits(a: str, b: str) -> int:
     n = 0
     for x, y in zip(a, b):

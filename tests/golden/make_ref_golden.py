@@ -12,7 +12,6 @@ import argparse
 import json
 import os
 import sys
-from fractions import Fraction
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -25,11 +24,11 @@ BIG = [100000000]
 
 
 def dd_hex(hi: float, lo: float) -> str:
-    """The exact value hi+lo in [0,1) as 28 hex digits and 20 zeros (the
-    reference's mode-0 print form, 14 bytes)."""
-    x = (Fraction(hi) + Fraction(lo)) % 1
-    v = int(x * (1 << 112))
-    return format(v, "028x") + "0" * 20
+    """The reference's mode-0 print form of its double-double result: its
+    printer hexadecimal_dd (hexsademical.as:21-101) as restated in the oracle
+    (28 hex digits and 20 zeros)."""
+    from oracle import oracle as O
+    return O.hexadecimal_dd(hi, lo)
 
 
 def main():
@@ -51,6 +50,8 @@ def main():
             e = data.setdefault(str(p), {})
             e["d"] = r["d"]
             e["mode%d" % prec] = dd_hex(*r["dd"]) if prec == 0 else r["hex"]
+            if prec == 0:                    # the raw double-double, exactly (float.hex)
+                e["mode0_dd"] = [r["dd"][0].hex(), r["dd"][1].hex()]
             e["mode%d_seconds" % prec] = r["seconds"]
             e["threads"] = r.get("threads")
             json.dump(data, open(path, "w"), indent=1, sort_keys=True)

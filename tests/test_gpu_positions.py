@@ -195,9 +195,10 @@ def test_against_reference_kernels(ctx192, ctxdd):
         if not p.isdigit():
             continue
         h = ctx192.compute(int(p))
-        assert agree(h, e["mode2"]) >= 24, p
-        assert agree(h, e["mode1"]) >= 24, p
-        if int(p) <= 10 ** 7:
+        for mode in ("mode1", "mode2"):
+            if mode in e:
+                assert agree(h, e[mode]) >= 24, (p, mode)
+        if int(p) <= 10 ** 7 and "mode0" in e:
             assert agree(ctxdd.compute(int(p)), e["mode0"]) >= 19, p
 
 
