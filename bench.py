@@ -378,10 +378,13 @@ def ours_arm(args):
 
 
 def issue_fraction(kernel_ms: float):
-    """FMA-heavy pipe issue of the term kernel at 1e10, from a committed ncu
-    count (profiles/terms192_issue.json: warp instructions per launch on that
-    pipe and its peak of one warp instruction per 2 cycles per SM
-    sub-partition), against this run's kernel time at the profile's clock."""
+    """The FMA-heavy pipe (integer multiplies) of the term kernel at 1e10
+    from a committed one-pass ncu capture of the same workload
+    (profiles/terms192_issue.json): its busy fraction as ncu reports it, and
+    its warp-instruction issue rate against one warp instruction per 2 cycles
+    per SM sub-partition, with this run's kernel time at the profile's clock.
+    Wide and high multiplies hold the pipe for two issue cycles, so the busy
+    fraction is the higher of the two."""
     path = os.path.join(ROOT, "profiles", "terms192_issue.json")
     try:
         with open(path) as f:
@@ -390,7 +393,8 @@ def issue_fraction(kernel_ms: float):
         return None
     peak = p["sms"] * p["smsp_per_sm"] * p["warp_inst_per_cycle_per_smsp"] * p["sm_mhz"] * 1e6
     rate = p["fmaheavy_warp_inst_per_launch"] / (kernel_ms / 1000.0)
-    return {"fmaheavy_warp_inst_per_launch": p["fmaheavy_warp_inst_per_launch"],
+    return {"fmaheavy_pipe_busy_ncu": p["fmaheavy_pipe_busy_pct"] / 100.0,
+            "fmaheavy_warp_inst_per_launch": p["fmaheavy_warp_inst_per_launch"],
             "fmaheavy_issue_frac": rate / peak, "source": p.get("source", path)}
 
 
