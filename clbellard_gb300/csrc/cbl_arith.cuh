@@ -234,17 +234,17 @@ struct W1SState {
 
 
 // ------------------------------------------------------ middle width 1 --
-// 2^28 <= m < 2^31: R = 2^32, residues in [0, m). y^2 + u m < 2^64, so the
-// reduction is one word step with no carry out; REDC < 2m and the doubling
-// < 2m are brought back below m by min(x, x - m).
+// 2^28 <= m < 2^31: R = 2^32, residues in [0, m). The doubling comes first:
+// t = y (2^b y) < 2m^2 < 2^63 and u m < 2^63, so the word step has no carry
+// out and REDC(t) = REDC(y^2) 2^b mod m is below 2m; one min(z, z - m)
+// brings it below m. (Two ALU operations fewer than reducing, then doubling
+// and reducing again.)
 __device__ __forceinline__ uint32_t w1m_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
 {
-    const uint64_t t = (uint64_t)y * y;
+    const uint64_t t = (uint64_t)y * (y << b);
     const uint32_t u = (uint32_t)t * mp;
     const uint32_t z = redc_word(u, m, (uint32_t)t, (uint32_t)(t >> 32));   // < 2m
-    const uint32_t r = min(z, z - m);                               // < m < 2^31
-    const uint32_t x = r << b;                                      // < 2m
-    return min(x, x - m);
+    return min(z, z - m);
 }
 
 struct W1MState {
