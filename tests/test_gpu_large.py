@@ -62,3 +62,31 @@ def test_1e11_overlap_and_split(ctx192):
     assert h == a
     from clbellard_gb300 import workmode_sum
     assert workmode_sum([ctx192.run_job(10 ** 11, s, 0) for s in range(7)]) == h
+
+
+def test_1e11_checkpointed_passes_against_oracle(cbl):
+    """Config 5: position 1e11 (moduli up to 2^38.6, the two-word kinds
+    throughout the upper range) run as time-budgeted passes; after the first
+    slice the checkpoint is restored into a fresh context, as after a crash,
+    and the pass continues. The result equals the exact oracle's 192-bit
+    value bit for bit and its 256-bit value for >= 30 hex digits."""
+    fixtures = load_golden("oracle_big.json")
+    if "100000000000" not in fixtures:
+        pytest.skip("no exact 1e11 fixture (tests/golden/make_golden.py --big 100000000000)")
+    big = fixtures["100000000000"]
+    with cbl.Context(0, 1) as ctx:
+        ctx.prepare([10 ** 11])
+        done, total = ctx.run_prepared_budget(2000.0)
+        assert 0 < done < total
+        blob = ctx.checkpoint()
+    with cbl.Context(0, 1) as ctx:
+        ctx.prepare([10 ** 11])
+        ctx.restore(blob)
+        slices = 1
+        while done < total:
+            done, total = ctx.run_prepared_budget(2000.0)
+            slices += 1
+        h = "%048x" % ctx.read_results()[0]
+    assert slices >= 3
+    assert h == big["hex192"]
+    assert agree(h, big["hex256"]) >= 30
