@@ -441,8 +441,10 @@ def split_arm(args, world, rank, local):
         "config": workload_config(d),
         "launch": {"split": "%d balanced jobs (cbl_plan_jobs), %d per rank, merged by an exact 48-hex add"
                             % (8 * world, 8)},
-        "e2e": {"value": 7 * d / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 24 * 8, "note": "host wall time including the job partials' merge"},
+        "e2e": {"value": 7 * d / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 48 * 7 * 8,
+                "d2h_bytes_per_step": 24 * 8,
+                "note": "host wall time including the job partials' merge; h2d is the bound of 8 jobs' segment "
+                        "tables (48 B per segment, at most 7 per job), d2h the 8 partials"},
         "gpu_launches": launches,
         "result_hex": merged,
         "result_equals_oracle": (merged == exact["hex192"]) if exact else None,
