@@ -211,20 +211,22 @@ __device__ __forceinline__ uint32_t w1_digits(uint32_t r, uint32_t m, uint32_t m
 }
 
 // --------------------------------------------------------- strict width 1 --
-// 2^31 <= m < 2^32: R = 2^32, residues in [0, m). u m + y^2 can pass 2^64
-// once: the carry chain returns the carry c out of the high word, and
-// REDC = x + c 2^32 < 2m. The doubling's carry out of bit 31 comes from a
-// funnel shift. (Valid for 2^28 <= m < 2^32.)
+// 2^31 <= m < 2^32: R = 2^32, residues in [0, m). The doubling comes first,
+// into the second multiplicand only: y2 = 2^b y, less m when the shift carries
+// out of bit 31, is below 2^32 (not necessarily below m), so t = y y2 < m 2^32.
+// u m + t can pass 2^64 once: the carry chain returns the carry c out of the
+// high word, REDC = x + c 2^32 < 2m, and one conditional subtraction brings it
+// below m. (Valid for 2^28 <= m < 2^32.)
 __device__ __forceinline__ uint32_t w1s_sqr(uint32_t y, uint32_t m, uint32_t mp, uint32_t b)
 {
-    const uint64_t t = (uint64_t)y * y;
+    const uint32_t x2 = y << b;
+    const uint32_t c2 = __funnelshift_l(y, 0u, b);                 // bit shifted out of y
+    const uint32_t y2 = c2 ? x2 - m : x2;                          // 2^b y mod m, < 2^32
+    const uint64_t t = (uint64_t)y * y2;
     const uint32_t u = (uint32_t)t * mp;
     uint32_t c;
     const uint32_t x = redc_word_c(u, m, (uint32_t)t, (uint32_t)(t >> 32), c);
-    const uint32_t r = c ? x - m : min(x, x - m);                  // REDC mod m, in [0, m)
-    const uint32_t x2 = r << b;
-    const uint32_t c2 = __funnelshift_l(r, 0u, b);                 // bit shifted out of r
-    return c2 ? x2 - m : min(x2, x2 - m);                          // 2^b r mod m
+    return c ? x - m : min(x, x - m);                              // REDC mod m, in [0, m)
 }
 
 struct W1SState {
