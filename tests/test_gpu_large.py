@@ -27,7 +27,7 @@ def test_1e10(ctx192):
 
 
 def test_1e10_against_reference_192bit_output(ctx192):
-    """The spec bar: at position 1e10 the GPU's hex digits match the
+    """The target for this path: at position 1e10 the GPU's hex digits match the
     reference's own 192-bit output (its kernels run in full on the CPU,
     precision 2) for >= 24 digits; they agree for 38."""
     ref = load_golden("ref_outputs.json")["10000000000"]

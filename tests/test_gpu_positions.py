@@ -188,7 +188,7 @@ def test_launch_count_counts_kernels(ctx192):
 
 def test_against_reference_kernels(ctx192, ctxdd):
     """GPU results against the reference's own kernels run on the CPU: the
-    192-bit modes agree for >= 24 hex digits (the spec bar), the
+    192-bit modes agree for >= 24 hex digits (the target for this path), the
     106-bit mode for >= 19."""
     ref = load_golden("ref_outputs.json")
     for p, e in ref.items():
