@@ -31,6 +31,13 @@ def test_reference_arm_two_ranks():
     assert rec["impl"] == "reference" and rec["n_gpus"] == 2 and rec["value"] > 0
     assert rec["cpu_baseline"]["kind"] in ("reference", "port") and rec["cpu_baseline"]["value"] == rec["value"]
     assert rec["e2e"]["h2d_bytes_per_step"] == 0 and rec["e2e"]["value"] == rec["value"]
+    # the same config as the GPU arm, key for key; what was timed, and what is extrapolated
+    sys.path.insert(0, ROOT)
+    import bench
+    assert rec["config"] == bench.workload_config(3999999999)
+    assert rec["extrapolated"] is True and rec["timed_s"] > 0 and rec["terms_timed"] > 0
+    assert abs(rec["value"] - rec["terms_timed"] / rec["timed_s"]) <= 1e-6 * rec["value"]
+    assert rec["ms_per_position_extrapolated"] > rec["ms_per_step"]
 
 
 def _rank(rank, port, q):
