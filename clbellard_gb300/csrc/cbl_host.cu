@@ -957,19 +957,18 @@ int cbl_run_job(cbl_ctx *c, uint64_t needD, int s, uint64_t b, uint64_t batchsiz
 }
 
 // ---- balanced work-mode planning
-// Relative cost of one ladder step per residue kind (instructions per step
-// measured with ncu on GB300: about 7, 10, 13, 25, 28, 30).
 // Relative cost of one ladder step per residue kind, from each kind's measured
-// term rate on its own k-range (GB300): W1 7, W1M 9, W1S 11, W2S 18, W2 21;
-// W2X adds one 64-bit min to the W2 step.
+// term time on its own k-range (GB300; 0.6e8-4.6e8 terms per range, divided by
+// bitlen(10(d-k)) + 8 and scaled to W1 = 7): W1 7, W1M 5.9, W1S 8.2, W2S 14.5,
+// W2 16.8, W2X 24.3.
 static double step_cost(uint64_t m)
 {
     if (m < kW1Max) return 7.0;
-    if (m < kW1MMax) return 9.0;
-    if (m < kW1SMax) return 11.0;
-    if (m < kW2SMax) return 18.0;
-    if (m < kW2Max) return 21.0;
-    return 22.0;
+    if (m < kW1MMax) return 5.9;
+    if (m < kW1SMax) return 8.2;
+    if (m < kW2SMax) return 14.5;
+    if (m < kW2Max) return 16.8;
+    return 24.3;
 }
 
 // Estimated cost of terms k in [k0, k1) of series f at position d (k < d):
