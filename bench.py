@@ -117,36 +117,44 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- CPU baseline --
-def cpu_sample_rate(needD: int, target_s: float, threads: int = 0):
+def _cpu_sample(d: int, L: int, threads: int):
+    """The oracle over 7 series x 16 chunks of L terms spread evenly over
+    k in [0, d): (terms, seconds)."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    n = 0
+    for f in range(7):
+        for j in range(16):
+            k0 = (d * j) // 16
+            O.sum_range(d, f, k0, min(d, k0 + L), 3, threads)
+            n += min(d, k0 + L) - k0
+    return n, time.perf_counter() - t0
+
+
+def cpu_sample_size(d: int, target_s: float, threads: int = 0) -> int:
+    """Chunk length L for a sample of about target_s, from a probe that runs at
+    least 0.5 s."""
+    L = 4096
+    while True:
+        n, t = _cpu_sample(d, L, threads)
+        if t >= 0.5 or L >= d:
+            break
+        L = min(d, int(L * max(2.0, 0.6 / max(t, 1e-3))))
+    return max(256, min(d, int(n / max(t, 1e-6) * target_s / (7 * 16))))
+
+
+def cpu_sample_rate(needD: int, target_s: float, threads: int = 0, L: int = 0):
     """The oracle (CPU restatement of the reference's path) on a bounded,
     stratified sample of the workload: per series, 16 chunks spread evenly
-    over k in [0, d). The chunk length is sized from a probe that runs at
-    least 0.5 s, so the sample itself takes about target_s. Returns (terms/s,
-    sample description, cores, seconds timed, terms timed)."""
+    over k in [0, d), sized (unless L is given) so the sample takes about
+    target_s. Returns (terms/s, sample description, cores, seconds timed,
+    terms timed)."""
     from oracle import oracle as O
     O.build()
     d, _ = O.pos_to_d(needD)
     cores = threads or os.cpu_count() or 1
-
-    def run(L):
-        t0 = time.perf_counter()
-        n = 0
-        for f in range(7):
-            for j in range(16):
-                k0 = (d * j) // 16
-                O.sum_range(d, f, k0, min(d, k0 + L), 3, threads)
-                n += min(d, k0 + L) - k0
-        return n, time.perf_counter() - t0
-
-    L = 4096
-    while True:
-        n, t = run(L)
-        if t >= 0.5 or L >= d:
-            break
-        L = min(d, int(L * max(2.0, 0.6 / max(t, 1e-3))))
-    rate = n / max(t, 1e-6)
-    L = max(256, min(d, int(rate * target_s / (7 * 16))))
-    n, t = run(L)
+    L = L or cpu_sample_size(d, target_s, threads)
+    n, t = _cpu_sample(d, L, threads)
     return (n / t, "7 series x 16 chunks of %d k spread over [0,d) at position %d (%d terms, %.1f s)"
             % (L, needD, n, t), cores, t, n)
 
@@ -228,12 +236,14 @@ def reference_arm(args):
         L = max(1 << 16, int(rate * args.ref_seconds / 56))
         desc = ("reference kernels (precision 2) on 7 series x 8 chunks of %d k spread over [0,d) at position %d"
                 % (L, POSITION))
+    else:
+        L = cpu_sample_size(d, args.ref_seconds, threads)
     step_s, step_terms = [], []
     for i in range(args.warmup + args.steps):
         if use_ref:
             rate, t, n, cores = reference_sample(POSITION, L, threads)
         else:
-            rate, desc, cores, t, n = cpu_sample_rate(POSITION, args.ref_seconds, threads)
+            rate, desc, cores, t, n = cpu_sample_rate(POSITION, args.ref_seconds, threads, L)
             desc += ("; the reference's OpenCL/HSP host cannot run here and its kernels were not compiled for "
                      "this machine, so its CPU restatement (oracle/, Montgomery + exact long division) is timed")
         if i >= args.warmup:
