@@ -187,9 +187,9 @@ def test_launch_count_counts_kernels(ctx192):
 
 
 def test_against_reference_kernels(ctx192, ctxdd):
-    """GPU results against the reference's own kernels run on the CPU: the
-    192-bit modes agree for >= 24 hex digits (the target for this path), the
-    106-bit mode for >= 19."""
+    """GPU results against the reference's own kernels run on the CPU (up to
+    position 1e10 in full): the 192-bit modes agree for >= 24 hex digits (the
+    target for this path), the 106-bit mode for >= 19."""
     ref = load_golden("ref_outputs.json")
     for p, e in ref.items():
         if not p.isdigit():
@@ -198,7 +198,7 @@ def test_against_reference_kernels(ctx192, ctxdd):
         for mode in ("mode1", "mode2"):
             if mode in e:
                 assert agree(h, e[mode]) >= 24, (p, mode)
-        if int(p) <= 10 ** 7 and "mode0" in e:
+        if "mode0" in e:
             assert agree(ctxdd.compute(int(p)), e["mode0"]) >= 19, p
 
 
