@@ -368,6 +368,10 @@ def ours_arm(args):
         "result_equals_oracle": (result == exact["hex192"]) if exact else None,
         "clocks": clk.summary(),
     }
+    ref = golden("ref_outputs.json").get(str(needD), {})
+    if "mode2" in ref:
+        # the reference's own 192-bit output at this position (its kernels run in full on a CPU)
+        line["digits_equal_to_reference_192bit"] = agreeing_digits(result, ref["mode2"])
     pipe = issue_fraction(kms)
     if pipe:
         line["roofline"]["pipe"] = pipe
@@ -598,6 +602,9 @@ def dd_digits(C, device, needD, h192, exact):
         hdd = ctxdd.compute(needD)
         ms = (time.perf_counter() - t0) * 1000.0
     r = {"position": needD, "hex_dd": hdd, "ms_dd": ms, "digits_vs_192": agreeing_digits(hdd, h192)}
+    ref = golden("ref_outputs.json").get(str(needD), {})
+    if "mode0" in ref:
+        r["digits_vs_reference_mode0"] = agreeing_digits(hdd, ref["mode0"])
     if exact:
         r["digits_vs_exact_256"] = agreeing_digits(hdd, exact["hex256"])
         r["digits_192_vs_exact_256"] = agreeing_digits(h192, exact["hex256"])
