@@ -103,7 +103,8 @@ def test_big_fixture_consistency():
     s = load_golden("recorded_probe.json")
     pub = load_golden("published_digits.json")["digits"]
     for p, v in g.items():
-        assert v["hex256"].startswith(pub[p])
+        if p in pub:
+            assert v["hex256"].startswith(pub[p])
         assert agree(v["hex192"], v["hex256"]) >= 33
         if p in s["exact256"]:
             assert agree(v["hex256"], s["exact256"][p]) >= 48
